@@ -1,0 +1,303 @@
+"""Benchmark: Mrays/s of the GB300 path tracer on the icosphere workload.
+
+Workload (one step = one frame): Cornell box + seeded noise-displaced
+icosphere, subdivision 7 (327,680 + 34 triangles), 24 random metallic-
+roughness materials, 4 point lights, 1920x1080, 64 samples per pixel, 8
+bounces, Russian roulette after bounce 3.  Each step renders the next 64
+samples into the resident accumulation buffer (progressive accumulation like
+the reference's frame loop), so no step repeats another's work.
+
+Rays counted: camera, extension and shadow segments (every traced segment
+once).  `value` is device throughput with the scene resident in HBM, timed
+with CUDA events on the library's stream; L2 (the scene is ~60 MB, below the
+129 MB L2) is flushed between steps by writing a 256 MiB buffer.  `e2e` is
+the same metric through the public C-ABI call gbrt_render with a host UBO in
+and the tone-mapped RGBA8 image copied back to host memory every step.
+
+--impl reference times the CPU oracle (the C++ restatement of the reference
+shaders, all host threads) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, SPP, DEPTH, SUBDIV = 1920, 1080, 64, 8, 7
+WORKLOAD = f"icosphere{SUBDIV}_cornell_{W}x{H}_{SPP}spp_depth{DEPTH}"
+B_SHADE = 608  # algorithmic bytes per shaded hit (index, PrimInfo, 3 vertex subsets, material, new ray, path state)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while
+    the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3][0].isdigit())}
+
+
+def make_scene():
+    from rustracer_gb300 import scenes
+    return scenes.icosphere_scene(subdiv=SUBDIV)
+
+
+def cpu_sample(sd, threads=0, target_s=12.0, rows=None):
+    """Times the CPU oracle on a bounded sample of the workload: the full
+    1920x1080 frame at 1 spp first (also the ray set for the N_node/N_tri
+    statistics), repeated with more samples if that was much shorter than
+    target_s.  Returns (result dict, stats)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    o = O.OracleScene(sd)
+    r0, r1 = rows if rows else (0, H)
+    spp = 1
+    while True:
+        ubo = sd.ubo(W, H, samples=spp, bounces=DEPTH, exposure=1.0)
+        st = o.render(ubo, W, H, rows=(r0, r1), threads=threads, out=False)["stats"]
+        if st["seconds"] >= target_s / 3 or spp >= SPP:
+            break
+        spp = min(SPP, max(spp * 2, int(spp * target_s / max(st["seconds"], 1e-3))))
+    rays = int(st["rays_camera"] + st["rays_extension"] + st["rays_shadow"])
+    return {"rays": rays, "seconds": float(st["seconds"]), "threads": int(st["threads"]), "spp": spp,
+            "rows": (r0, r1), "node_visits": int(st["node_visits"]), "tri_tests": int(st["tri_tests"]),
+            "hits_shaded": int(st["hits_shaded"])}
+
+
+def b_ray(cs):
+    """Algorithmic bytes per ray: 32 (ray) + 16 (hit) + N_node*64 + N_tri*36,
+    N_node / N_tri the mean BVH2 inner-node visits and triangle tests per ray
+    of the oracle's binned-SAH BVH2 on the same ray set."""
+    n_node = cs["node_visits"] / cs["rays"]
+    n_tri = cs["tri_tests"] / cs["rays"]
+    return 48.0 + 64.0 * n_node + 36.0 * n_tri, n_node, n_tri
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def common_line(args, n, value, ms_per_step, extra_cfg=None):
+    cfg = {"workload": WORKLOAD, "width": W, "height": H, "spp_per_step": SPP, "depth": DEPTH,
+           "triangles": 20 * 4 ** SUBDIV + 34, "materials": 24 + 4, "point_lights": 4,
+           "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas{n}" if n > 1 else "single"}
+    if extra_cfg:
+        cfg.update(extra_cfg)
+    return {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": n, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere + Cornell box)",
+            "config": cfg}
+
+
+def traffic_from_profile():
+    """dram bytes per launch of pt_megakernel from the committed ncu summary
+    (profiles/pt_megakernel_icosphere.json), scaled to one full launch."""
+    p = os.path.join(ROOT, "profiles", "pt_megakernel_icosphere.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get("dram_bytes_per_full_launch")
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from rustracer_gb300 import build, gbrt
+    build.build()
+    sd = make_scene()
+    ctx = gbrt.Context(local)
+    scene = gbrt.Scene(ctx, sd)
+    acc = gbrt.Accum(ctx, W, H)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
+    state = {"total": 0}
+
+    def frame(out_ptr=None):
+        state["total"] += SPP
+        ubo = np.asarray(sd.ubo(W, H, samples=SPP, total=state["total"], bounces=DEPTH, exposure=1.0)).reshape(())
+        st = np.zeros((), gbrt.T.STATS)
+        ctx.check(ctx.L.gbrt_render(scene.h, gbrt._p(ubo), acc.h, out_ptr, gbrt._p(st)))
+        return st
+
+    def flush_l2():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        flush_l2()
+        frame()
+    barrier()
+    rays = shaded = 0
+    dev_ms = 0.0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush_l2()
+            st = frame()
+            rays += int(st["rays_total"])
+            shaded += int(st["hits_shaded"])
+            dev_ms += float(st["device_ms"])
+        barrier()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    # end to end through the C ABI: UBO in, RGBA8 image out to pinned host memory
+    e2e_rays, e2e_s = 0, 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        t = time.perf_counter()
+        st = frame(pinned.data_ptr())
+        e2e_s += time.perf_counter() - t
+        e2e_rays += int(st["rays_total"])
+
+    stats = torch.tensor([dev_ms, wall, e2e_s, float(rays), float(e2e_rays)], dtype=torch.float64,
+                         device=f"cuda:{local}")
+    if world > 1:
+        import torch.distributed as dist
+        mx = stats.clone()
+        dist.all_reduce(mx[:3], op=dist.ReduceOp.MAX)
+        sm = stats.clone()
+        dist.all_reduce(sm[3:], op=dist.ReduceOp.SUM)
+        dev_ms, wall, e2e_s = (float(x) for x in mx[:3])
+        tot_rays, tot_e2e = float(sm[3]), float(sm[4])
+    else:
+        tot_rays, tot_e2e = float(rays), float(e2e_rays)
+    if rank != 0:
+        return
+    cs = cpu_sample(sd, target_s=args.cpu_seconds) if world == 1 else cpu_sample(sd, target_s=0.0)
+    bray, n_node, n_tri = b_ray(cs)
+    value = tot_rays / (dev_ms / 1e3) / 1e6
+    peak, peak_kind = measured_peaks()
+    per_launch_bytes = (rays * bray + shaded * B_SHADE) / args.steps
+    achieved = per_launch_bytes / (dev_ms / args.steps / 1e3) / 1e9
+    traffic = traffic_from_profile()
+    line = common_line(args, world, value, dev_ms / args.steps,
+                       {"kernel": "pt_megakernel", "wall_ms_per_step": wall / args.steps * 1e3})
+    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": traffic, "peak_source": peak_kind,
+                        "bytes_per_ray": bray, "n_node": n_node, "n_tri": n_tri,
+                        "bytes_per_shaded_hit": B_SHADE, "kernel": "pt_megakernel",
+                        "hbm_roofline_mrays": peak * 1e3 / bray}
+    line["e2e"] = {"value": tot_e2e / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(gbrt.T.UBO.itemsize),
+                   "d2h_bytes_per_step": W * H * 4}
+    if world == 1:
+        line["cpu_baseline"] = {"value": cs["rays"] / cs["seconds"] / 1e6, "unit": "Mrays/s", "cores": cs["threads"],
+                                "kind": "port",
+                                "sample": f"{W}x{H} frame at {cs['spp']} spp ({cs['rays']} rays, "
+                                          f"{cs['seconds']:.1f} s), same scene and depth"}
+    line["clocks"] = clocks
+    line["gpu_launches"] = args.steps
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sd = make_scene()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    o = O.OracleScene(sd)
+    ubo = sd.ubo(W, H, samples=1, bounces=DEPTH, exposure=1.0)
+    for _ in range(args.warmup):
+        o.render(ubo, W, H, rows=(0, H // 8), out=False)
+    rays, secs, threads = 0, 0.0, 1
+    for k in range(args.steps):
+        u = sd.ubo(W, H, samples=1, total=k + 1, bounces=DEPTH, exposure=1.0)
+        st = o.render(u, W, H, out=False)["stats"]
+        rays += int(st["rays_camera"] + st["rays_extension"] + st["rays_shadow"])
+        secs += float(st["seconds"])
+        threads = int(st["threads"])
+    value = rays / secs / 1e6
+    line = common_line(args, world, value, secs / args.steps * 1e3,
+                       {"kernel": "CPU oracle (C++ restatement of the reference shaders, OpenMP)",
+                        "step_sample": f"{W}x{H} frame at 1 spp (bounded sample of the 64-spp step)"})
+    line["impl"] = "reference"
+    line["cpu_baseline"] = {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                            "sample": f"{args.steps} x ({W}x{H} at 1 spp)"}
+    line["e2e"] = {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbrt", choices=["gbrt", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

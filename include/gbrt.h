@@ -1,0 +1,396 @@
+/*
+ * gbrt.h — C ABI of the GB300-native ray-tracing core.
+ *
+ * This header is the drop-in boundary for rustracer's Vulkan ray-tracing
+ * pipeline (KaminariOS/rustracer).  Every struct is plain C with fixed sizes so
+ * that a Rust host can mirror it with #[repr(C)]; every function returns an
+ * int status (0 = GBRT_OK, negative = GBRT_E_*), never throws and never
+ * aborts.  gbrt_last_error() gives the message of the last failure on a
+ * context.  Host arrays passed in stay owned by the caller; the library copies
+ * what it needs into device memory.
+ *
+ * Threading: a gbrt_ctx (and everything created from it) is used from one host
+ * thread at a time, except the job API (gbrt_job_*), which is internally
+ * locked.  All device work of a context runs on the context's CUDA stream.
+ *
+ * Citations below are paths inside the reference repository.
+ */
+#ifndef GBRT_H
+#define GBRT_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                             */
+/* ------------------------------------------------------------------------ */
+#define GBRT_OK               0
+#define GBRT_E_INVALID       -1  /* bad argument, size or state */
+#define GBRT_E_CUDA          -2  /* a CUDA runtime call failed */
+#define GBRT_E_OOM           -3  /* device allocation failed */
+#define GBRT_E_DEVICE_LIMIT  -4  /* a kernel hit an iteration/stack/queue cap */
+#define GBRT_E_NOT_BUILT     -5  /* render/trace before blas/tlas build */
+#define GBRT_E_NO_DEVICE     -6  /* no CUDA device, or the library was built without it */
+#define GBRT_E_BUSY          -7  /* job queue full / admission refused */
+
+/* ------------------------------------------------------------------------ */
+/* Data contract: byte-for-byte mirrors of the reference's #[repr(C)] types  */
+/* ------------------------------------------------------------------------ */
+
+/* Vertex, 128 B.  crates/libs/asset_loader/src/geometry.rs:10-22 and
+ * shaders/lib/RayTracingCommons.glsl:54-63.  pos.w is 0 on upload
+ * (geometry.rs:166); only pos.xyz is used by the BLAS build
+ * (acceleration_structures.rs:35-40, stride 128). */
+typedef struct gbrt_vertex {
+    float    pos[4];
+    float    normal[4];
+    float    tangent[4];
+    float    color[4];
+    float    weights[4];
+    uint32_t joints[4];
+    float    uv0[2];
+    float    uv1[2];
+    int32_t  skin_index;
+    uint32_t _pad[3];
+} gbrt_vertex;
+
+/* PrimInfo, 16 B: one per geometry (glTF primitive).  geometry.rs:65-73,
+ * RayTracingCommons.glsl:47-52. */
+typedef struct gbrt_priminfo {
+    uint32_t v_offset;
+    uint32_t i_offset;
+    uint32_t material_id;
+    uint32_t skin_id;
+} gbrt_priminfo;
+
+/* TextureInfo, 8 B.  material.rs:11-17; index -1 = no texture.  The
+ * reference offsets texture indices by +1 for its dummy texture 0
+ * (material.rs:36); the index here is the slot in the texture array given
+ * to gbrt_scene_create, which the host fills the same way. */
+typedef struct gbrt_texture_info {
+    int32_t index;
+    int32_t coord;
+} gbrt_texture_info;
+
+/* MaterialRaw, 256 B.  material.rs:130-160, shaders/lib/Material.glsl:51-73.
+ * alpha_mode: 1 = OPAQUE, 2 = MASK, 3 = BLEND as the shaders compare it
+ * (RayTracing.rahit:39-41).  workflow: 0 metallic-roughness, 1 specular-
+ * glossiness (material.rs:327-330). */
+typedef struct gbrt_material_raw {
+    uint32_t alpha_mode;                  /*   0 */
+    float    alpha_cutoff;                /*   4 */
+    uint32_t double_sided;                /*   8 */
+    uint32_t workflow;                    /*  12 */
+    float    _pad0[2];                    /*  16 */
+    gbrt_texture_info base_color_texture; /*  24 */
+    float    base_color[4];               /*  32 */
+    float    metallic_factor;             /*  48 */
+    float    roughness_factor;            /*  52 */
+    gbrt_texture_info metallic_roughness_texture; /* 56 */
+    gbrt_texture_info normal_texture;     /*  64 */
+    gbrt_texture_info emissive_texture;   /*  72 */
+    float    emissive_factor[4];          /*  80 */
+    gbrt_texture_info occlusion_texture;  /*  96 */
+    float    ior;                         /* 104 */
+    uint32_t unlit;                       /* 108 */
+    /* TransmissionInfo (material.rs:250-256) */
+    gbrt_texture_info transmission_texture; /* 112 */
+    float    transmission_factor;         /* 120 */
+    uint32_t transmission_exist;          /* 124 */
+    /* VolumeInfo (material.rs:193-201) */
+    float    attenuation_color[3];        /* 128 */
+    float    thickness_factor;            /* 140 */
+    gbrt_texture_info thickness_texture;  /* 144 */
+    float    attenuation_distance;        /* 152 */
+    uint32_t volume_exists;               /* 156 */
+    /* SpecularInfo (material.rs:290-299) */
+    gbrt_texture_info specular_texture;   /* 160 */
+    gbrt_texture_info specular_color_texture; /* 168 */
+    float    specular_color_factor[4];    /* 176 */
+    float    specular_factor;             /* 192 */
+    uint32_t specular_exist;              /* 196 */
+    uint32_t _pad1[2];                    /* 200 */
+    /* SpecularGlossiness (material.rs:268-276) */
+    float    sg_diffuse_factor[4];        /* 208 */
+    float    sg_specular_glossiness_factor[4]; /* 224: rgb specular, a glossiness */
+    gbrt_texture_info sg_diffuse_texture; /* 240 */
+    gbrt_texture_info sg_specular_glossiness_texture; /* 248 */
+} gbrt_material_raw;
+
+/* LightRaw, 48 B.  crates/libs/asset_loader/src/light.rs:62-71,
+ * shaders/lib/PunctualLight.glsl:8-15.  kind 0 directional (transform =
+ * direction), 1 point (transform = position); spot lights are uploaded as
+ * point lights (light.rs:51-57). */
+typedef struct gbrt_light_raw {
+    float    color[4];
+    float    transform[4];
+    uint32_t kind;
+    float    range;
+    float    intensity;
+    uint32_t _pad;
+} gbrt_light_raw;
+
+/* UniformBufferObject, 324 B.  crates/examples/gltf_viewer/src/ubo.rs:3-31,
+ * shaders/lib/UniformBufferObject.glsl:3-30.  Matrices are column-major. */
+typedef struct gbrt_ubo {
+    float    model_view[16];
+    float    projection[16];
+    float    model_view_inverse[16];
+    float    projection_inverse[16];
+    float    aperture;
+    float    focus_distance;
+    float    fov_angle;
+    float    orthographic_fov_dis;
+    float    heatmap_scale;
+    uint32_t total_number_of_samples;
+    uint32_t number_of_samples;
+    uint32_t number_of_bounces;
+    uint32_t random_seed;
+    uint32_t has_sky;
+    uint32_t antialiasing;
+    uint32_t mapping;
+    uint32_t frame_count;
+    uint32_t debug;
+    uint32_t fully_opaque;
+    float    exposure;
+    uint32_t tone_mapping_mode;
+} gbrt_ubo;
+
+/* Skin: 256 column-major joint matrices, 16 KiB.
+ * crates/libs/asset_loader/src/skinning.rs:9-10,53-57,
+ * shaders/AnimationCompute.comp:4-7. */
+#define GBRT_MAX_JOINTS 256
+typedef struct gbrt_skin_raw {
+    float joints[GBRT_MAX_JOINTS][16];
+} gbrt_skin_raw;
+
+/* TLAS instance, 64 B, laid out like VkAccelerationStructureInstanceKHR as
+ * the reference fills it (acceleration_structures.rs:153-167): row-major 3x4
+ * object-to-world transform, custom index (= geometry id) in the low 24 bits
+ * and the 8-bit mask in the high bits; sbt offset 24 bits + flags 8 bits;
+ * blas_handle = the geometry id whose BLAS this instance references. */
+typedef struct gbrt_instance {
+    float    transform[12];
+    uint32_t custom_index_and_mask;
+    uint32_t sbt_offset_and_flags;
+    uint64_t blas_handle;
+} gbrt_instance;
+
+/* One BLAS input per geometry: the range of vertices/indices it owns
+ * (GeoBuilder::len / offsets, geometry.rs:36-40) and whether its material is
+ * OPAQUE (geometry.rs:56-58 -> GeometryFlagsKHR::OPAQUE,
+ * acceleration_structures.rs:53-57). */
+typedef struct gbrt_geo_range {
+    uint32_t geo_id;
+    uint32_t v_len;
+    uint32_t i_len;
+    uint32_t opaque;
+} gbrt_geo_range;
+
+/* Texture image.  The reference decodes every texture to RGBA8 and samples
+ * it bilinearly without mips (crates/libs/vulkan/src/image.rs:48,102);
+ * colour textures are sRGB, the rest linear (material.rs:102-128). */
+#define GBRT_TEX_RGBA8_UNORM 0
+#define GBRT_TEX_RGBA8_SRGB  1
+#define GBRT_TEX_RGBA16F     2
+#define GBRT_WRAP_REPEAT          0
+#define GBRT_WRAP_CLAMP_TO_EDGE   1
+#define GBRT_WRAP_MIRRORED_REPEAT 2
+typedef struct gbrt_texture_desc {
+    uint32_t    width;
+    uint32_t    height;
+    uint32_t    format;   /* GBRT_TEX_* */
+    uint32_t    wrap_s;   /* GBRT_WRAP_* */
+    uint32_t    wrap_t;
+    uint32_t    _pad;
+    const void* data;     /* width*height texels, row-major, host memory */
+} gbrt_texture_desc;
+
+/* Ray query input / output for gbrt_trace_rays*.  A ray is 32 B. */
+typedef struct gbrt_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} gbrt_ray;
+
+/* instance_id = ~0u on a miss. */
+typedef struct gbrt_hit {
+    float    t;
+    float    u;           /* barycentric weight of vertex 1 (gl HitAttributes.x) */
+    float    v;           /* barycentric weight of vertex 2 */
+    uint32_t instance_id; /* gl_InstanceID */
+    uint32_t primitive_id;/* gl_PrimitiveID */
+    uint32_t custom_index;/* gl_InstanceCustomIndexEXT = geometry id */
+} gbrt_hit;
+
+/* Ray flags for gbrt_trace_rays* (subset of gl_RayFlags*). */
+#define GBRT_RAY_OPAQUE              0x01u  /* skip any-hit alpha tests */
+#define GBRT_RAY_TERMINATE_ON_FIRST  0x04u  /* shadow/occlusion query */
+
+/* Per-call statistics. */
+typedef struct gbrt_stats {
+    uint64_t rays_total;      /* camera + extension + shadow segments */
+    uint64_t rays_camera;
+    uint64_t rays_extension;
+    uint64_t rays_shadow;
+    uint64_t hits_shaded;
+    double   device_ms;       /* CUDA-event time of the device work */
+    uint32_t kernel_launches;
+    uint32_t device_status;   /* 0, or GBRT_STATUS_* bits reported by kernels */
+} gbrt_stats;
+
+#define GBRT_STATUS_STACK_OVERFLOW 0x1u
+#define GBRT_STATUS_ITER_LIMIT     0x2u
+#define GBRT_STATUS_QUEUE_OVERFLOW 0x4u
+
+/* Render options for gbrt_render_ex. */
+#define GBRT_MODE_AUTO       0
+#define GBRT_MODE_MEGAKERNEL 1
+#define GBRT_MODE_WAVEFRONT  2
+typedef struct gbrt_render_opts {
+    uint32_t mode;            /* GBRT_MODE_* */
+    uint32_t flags;           /* reserved, 0 */
+    /* Optional debug outputs (host memory, may be NULL):
+     * sample_radiance: width*height*number_of_samples*3 floats, per-sample
+     *                  path radiance, laid out [pixel][sample][rgb];
+     * primary_hits:    width*height*number_of_samples primary-ray hits. */
+    float*    sample_radiance;
+    gbrt_hit* primary_hits;
+} gbrt_render_opts;
+
+/* ------------------------------------------------------------------------ */
+/* Opaque handles                                                           */
+/* ------------------------------------------------------------------------ */
+typedef struct gbrt_ctx   gbrt_ctx;
+typedef struct gbrt_scene gbrt_scene;
+typedef struct gbrt_accum gbrt_accum;
+
+/* ------------------------------------------------------------------------ */
+/* Context                                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device` with its own stream.  Replaces
+ * the Vulkan Context creation in crates/libs/app/src/lib.rs:272-292. */
+int gbrt_ctx_create(int device, gbrt_ctx** out);
+int gbrt_ctx_destroy(gbrt_ctx* ctx);
+/* Message of the last failed call on ctx ("" if none).  ctx may be NULL for
+ * errors of gbrt_ctx_create. */
+const char* gbrt_last_error(const gbrt_ctx* ctx);
+/* Free / total device memory as seen by this context. */
+int gbrt_ctx_mem_info(gbrt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
+/* Waits for all work queued on the context's stream. */
+int gbrt_sync(gbrt_ctx* ctx);
+/* Library version string, e.g. "gbrt 0.1 sm_103a". */
+const char* gbrt_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Scene                                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Uploads the scene's device buffer set.  Replaces Buffers::new
+ * (crates/libs/asset_loader/src/globals.rs:44-152) and the texture upload of
+ * create_global (globals.rs:309-350).  ni must be a multiple of 3 for every
+ * geometry's index range.  Textures may be NULL when ntex = 0. */
+int gbrt_scene_create(gbrt_ctx* ctx,
+                      const gbrt_vertex* vertices, uint32_t nv,
+                      const uint32_t* indices, uint32_t ni,
+                      const gbrt_priminfo* prims, uint32_t ngeo,
+                      const gbrt_material_raw* materials, uint32_t nmat,
+                      const gbrt_texture_desc* textures, uint32_t ntex,
+                      gbrt_scene** out);
+int gbrt_scene_destroy(gbrt_scene* scene);
+
+/* Builds one BLAS per geometry range on the GPU (Morton LBVH).  Replaces the
+ * per-primitive vkCmdBuildAccelerationStructuresKHR of create_as
+ * (acceleration_structures.rs:17-76,79-111).  flags: reserved, 0. */
+int gbrt_blas_build(gbrt_scene* scene, const gbrt_geo_range* ranges, uint32_t n,
+                    uint32_t flags);
+
+/* Builds the TLAS over instances.  Replaces create_top_as
+ * (acceleration_structures.rs:136-249).  Instances whose transform is the
+ * identity are merged into one world-space BVH; the others are traversed
+ * two-level through their geometry's BLAS. */
+int gbrt_tlas_build(gbrt_scene* scene, const gbrt_instance* instances, uint32_t n);
+
+/* Re-fits the TLAS for new instance transforms without a rebuild of the
+ * BLASes.  The reference rebuilds the TLAS every animated frame
+ * (crates/examples/gltf_viewer/src/main.rs:405-408). */
+int gbrt_tlas_update(gbrt_scene* scene, const gbrt_instance* instances, uint32_t n);
+
+/* Linear-blend skinning of every vertex with skin_index >= 0 (exactly
+ * shaders/AnimationCompute.comp:14-39, dispatched by
+ * crates/examples/gltf_viewer/src/compute_unit.rs:30-68), followed by a
+ * bottom-up refit of the BVHs that hold skinned geometry.  The reference
+ * does a full BLAS+TLAS rebuild instead (main.rs:383-404). */
+int gbrt_skin_and_refit(gbrt_scene* scene, const gbrt_skin_raw* skins, uint32_t nskin);
+
+/* Directional and point lights.  Replaces the dlights/plights buffers
+ * (globals.rs:111-125) and their per-frame update (main.rs:353-374). */
+int gbrt_lights_set(gbrt_scene* scene,
+                    const gbrt_light_raw* dir_lights, uint32_t nd,
+                    const gbrt_light_raw* point_lights, uint32_t np);
+
+/* Skybox cubemap: 6 square RGBA8 (sRGB-encoded) faces of face_size^2 texels
+ * in the order +X,-X,+Y,-Y,+Z,-Z (globals.rs:175-199).  NULL clears it. */
+int gbrt_skybox_set(gbrt_scene* scene, uint32_t face_size, const uint8_t* rgba8_faces);
+
+/* ------------------------------------------------------------------------ */
+/* Accumulation image                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* Device-resident RGBA32F running sum, like the reference's acc_image
+ * (crates/libs/app/src/lib.rs:316-326) plus its sample count. */
+int gbrt_accum_create(gbrt_ctx* ctx, uint32_t width, uint32_t height, gbrt_accum** out);
+int gbrt_accum_reset(gbrt_accum* acc);
+/* Copies width*height*4 floats (the running sum) to host memory. */
+int gbrt_accum_download(gbrt_accum* acc, float* rgba32f);
+int gbrt_accum_destroy(gbrt_accum* acc);
+
+/* ------------------------------------------------------------------------ */
+/* Rendering and ray queries                                                */
+/* ------------------------------------------------------------------------ */
+
+/* Renders ubo->number_of_samples samples per pixel into acc and (if out is
+ * not NULL) writes the tone-mapped RGBA8 image (width*height*4 bytes) to
+ * host memory.  Replaces the UBO upload + vkCmdTraceRaysKHR of
+ * crates/examples/gltf_viewer/src/main.rs:215-270 and the shaders
+ * RayTracing.{rgen,rchit,rahit,rmiss}, shadow.{rahit,rmiss}.  Synchronous.
+ * stats may be NULL. */
+int gbrt_render(gbrt_scene* scene, const gbrt_ubo* ubo, gbrt_accum* acc,
+                uint8_t* out_rgba8, gbrt_stats* stats);
+/* Same with explicit options (kernel form, debug outputs). */
+int gbrt_render_ex(gbrt_scene* scene, const gbrt_ubo* ubo, gbrt_accum* acc,
+                   uint8_t* out_rgba8, gbrt_stats* stats, const gbrt_render_opts* opts);
+
+/* Closest-hit (or, with GBRT_RAY_TERMINATE_ON_FIRST, any-hit) queries for
+ * n rays in host memory; hits written to host memory.  This is traceRayEXT
+ * on its own (RayTracing.rgen:89-92, RayTracing.rchit:51-55). */
+int gbrt_trace_rays(gbrt_scene* scene, const gbrt_ray* rays, uint32_t n,
+                    uint32_t ray_flags, gbrt_hit* hits, gbrt_stats* stats);
+/* Same with rays and hits already in device memory, enqueued on the
+ * context's stream (asynchronous; call gbrt_sync before reading hits). */
+int gbrt_trace_rays_device(gbrt_scene* scene, const gbrt_ray* d_rays, uint32_t n,
+                           uint32_t ray_flags, gbrt_hit* d_hits);
+
+/* ------------------------------------------------------------------------ */
+/* Device memory helpers (for callers without a CUDA runtime of their own)  */
+/* ------------------------------------------------------------------------ */
+int gbrt_device_alloc(gbrt_ctx* ctx, uint64_t bytes, void** d_ptr);
+int gbrt_device_free(gbrt_ctx* ctx, void* d_ptr);
+int gbrt_memcpy_h2d(gbrt_ctx* ctx, void* d_dst, const void* h_src, uint64_t bytes);
+int gbrt_memcpy_d2h(gbrt_ctx* ctx, void* h_dst, const void* d_src, uint64_t bytes);
+
+/* CUDA-event timer on the context's stream (ms between begin and end). */
+int gbrt_timer_begin(gbrt_ctx* ctx);
+int gbrt_timer_end(gbrt_ctx* ctx, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBRT_H */

@@ -1,0 +1,758 @@
+// api.cu — host implementation of the C ABI in include/gbrt.h.
+//
+// Every entry point validates its arguments, records a message on failure,
+// returns a GBRT_* code and never throws across the ABI.  Device memory is
+// owned by the handle that created it and released by its *_destroy.
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+using namespace gbrt;
+
+static_assert(sizeof(gbrt_vertex) == 128, "Vertex is 128 B (geometry.rs:10-22)");
+static_assert(sizeof(gbrt_priminfo) == 16, "PrimInfo is 16 B");
+static_assert(sizeof(gbrt_material_raw) == 256, "MaterialRaw is 256 B");
+static_assert(offsetof(gbrt_material_raw, attenuation_color) == 128, "VolumeInfo at 128");
+static_assert(offsetof(gbrt_material_raw, specular_texture) == 160, "SpecularInfo at 160");
+static_assert(offsetof(gbrt_material_raw, sg_diffuse_factor) == 208, "SpecularGlossiness at 208");
+static_assert(sizeof(gbrt_light_raw) == 48, "LightRaw is 48 B");
+static_assert(sizeof(gbrt_ubo) == 324, "UniformBufferObject is 324 B");
+static_assert(sizeof(gbrt_instance) == 64, "VkAccelerationStructureInstanceKHR is 64 B");
+static_assert(sizeof(gbrt_skin_raw) == 16384, "Skin is 256 mat4");
+static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records");
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        if (n == bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    // grows only
+    cudaError_t reserve(size_t n) { return n <= bytes ? cudaSuccess : alloc(n); }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct gbrt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tb0 = nullptr, tb1 = nullptr;
+    std::string err;
+    DevBuf counters;
+    DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
+    std::mutex mu;
+};
+
+struct gbrt_scene {
+    gbrt_ctx* ctx = nullptr;
+    uint32_t nv = 0, ni = 0, ngeo = 0, nmat = 0, ntex = 0;
+    DevBuf vertices, base_vertices, indices, prims, mats, tex_descs, dlights, plights, sky, skins;
+    std::vector<DevBuf*> tex_data;
+    std::vector<gbrt_priminfo> h_prims;
+    std::vector<uint32_t> h_indices;     // for range validation
+    std::vector<gbrt_geo_range> ranges;  // by geo id
+    std::vector<uint8_t> has_range;
+    std::vector<gbrt_instance> instances;
+    uint32_t nd = 0, np = 0, sky_size = 0;
+    bool skinned = false;
+    bool all_opaque = true;
+    // acceleration structures
+    DevBuf nodes, tris, inst, items;
+    bool built = false;
+    DevScene view{};
+    ~gbrt_scene() {
+        for (DevBuf* b : tex_data) delete b;
+    }
+};
+
+struct gbrt_accum {
+    gbrt_ctx* ctx = nullptr;
+    uint32_t w = 0, h = 0;
+    DevBuf buf;
+};
+
+namespace {
+
+int fail(gbrt_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+int cuda_fail(gbrt_ctx* c, cudaError_t e, const char* what) {
+    cudaGetLastError();  // clear sticky-free errors
+    return fail(c, e == cudaErrorMemoryAllocation ? GBRT_E_OOM : GBRT_E_CUDA,
+                std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+#define CU(ctx, x, what)                                   \
+    do {                                                   \
+        cudaError_t e_ = (x);                              \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// World-to-object transform: adjugate inverse of the 3x3 part in double and
+// translation -R^-1 t, each rounded once to float (the oracle computes the
+// same expression).
+void affine_inverse(const float* m, float* inv) {
+    double a00 = m[0], a01 = m[1], a02 = m[2], a10 = m[4], a11 = m[5], a12 = m[6];
+    double a20 = m[8], a21 = m[9], a22 = m[10];
+    double t0 = m[3], t1 = m[7], t2 = m[11];
+    double det = a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+    double r[9] = {(a11 * a22 - a12 * a21) / det, (a02 * a21 - a01 * a22) / det, (a01 * a12 - a02 * a11) / det,
+                   (a12 * a20 - a10 * a22) / det, (a00 * a22 - a02 * a20) / det, (a02 * a10 - a00 * a12) / det,
+                   (a10 * a21 - a11 * a20) / det, (a01 * a20 - a00 * a21) / det, (a00 * a11 - a01 * a10) / det};
+    for (int i = 0; i < 3; ++i) {
+        inv[i * 4 + 0] = (float)r[i * 3 + 0];
+        inv[i * 4 + 1] = (float)r[i * 3 + 1];
+        inv[i * 4 + 2] = (float)r[i * 3 + 2];
+        inv[i * 4 + 3] = (float)(-(r[i * 3 + 0] * t0 + r[i * 3 + 1] * t1 + r[i * 3 + 2] * t2));
+    }
+}
+
+bool is_identity(const float* m) {
+    static const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    return std::memcmp(m, id, sizeof(id)) == 0;
+}
+
+template <class T>
+cudaError_t upload(DevBuf& b, const T* src, size_t n, cudaStream_t st) {
+    cudaError_t e = b.alloc(n * sizeof(T));
+    if (e != cudaSuccess || n == 0) return e;
+    return cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+void refresh_view(gbrt_scene* s) {
+    DevScene& v = s->view;
+    v.nodes = s->nodes.as<BNode2>();
+    v.tris = s->tris.as<TriRec>();
+    v.inst = s->inst.as<DevInstance>();
+    v.ninst = (uint32_t)s->instances.size();
+    v.vertices = s->vertices.as<gbrt_vertex>();
+    v.indices = s->indices.as<uint32_t>();
+    v.prims = s->prims.as<gbrt_priminfo>();
+    v.mats = s->mats.as<gbrt_material_raw>();
+    v.tex = s->tex_descs.as<DevTexture>();
+    v.ntex = s->ntex;
+    v.dlights = s->dlights.as<gbrt_light_raw>();
+    v.nd = s->nd;
+    v.plights = s->plights.as<gbrt_light_raw>();
+    v.np = s->np;
+    v.sky = s->sky.as<uchar4>();
+    v.sky_size = s->sky_size;
+}
+
+// Builds the merged world BVH, the BLASes of transformed instances and the
+// TLAS into fresh pools.
+int build_all(gbrt_scene* s) {
+    gbrt_ctx* c = s->ctx;
+    cudaStream_t st = c->stream;
+    const size_t ninst = s->instances.size();
+    std::vector<DevInstance> hinst(ninst);
+    std::vector<uint4> world_items;
+    std::vector<uint32_t> tlas_ids;
+    std::vector<uint8_t> blas_needed(s->ngeo, 0);
+    bool all_opaque = true;
+    for (size_t i = 0; i < ninst; ++i) {
+        const gbrt_instance& in = s->instances[i];
+        DevInstance& d = hinst[i];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.xf, in.transform, sizeof(d.xf));
+        affine_inverse(d.xf, d.inv);
+        d.custom = in.custom_index_and_mask & 0xFFFFFFu;
+        d.mask = in.custom_index_and_mask >> 24;
+        d.blas_geo = (uint32_t)in.blas_handle;
+        if (d.blas_geo >= s->ngeo || d.custom >= s->ngeo)
+            return fail(c, GBRT_E_INVALID, "instance " + std::to_string(i) + " references a geometry out of range");
+        if (!s->has_range[d.blas_geo])
+            return fail(c, GBRT_E_NOT_BUILT, "instance " + std::to_string(i) + " uses a geometry without a BLAS range");
+        const gbrt_geo_range& r = s->ranges[d.blas_geo];
+        const uint32_t ntri = r.i_len / 3;
+        // shading fetches triangles through PrimInfo[custom index]; it must
+        // cover every primitive id the BLAS can return
+        if (d.custom != d.blas_geo && (!s->has_range[d.custom] || s->ranges[d.custom].i_len < r.i_len))
+            return fail(c, GBRT_E_INVALID, "instance " + std::to_string(i) +
+                                               ": custom index geometry has fewer triangles than its BLAS");
+        d.identity = is_identity(in.transform) && (d.mask & 0xFFu) != 0;
+        if ((d.mask & 0xFFu) == 0 || ntri == 0) continue;
+        if (!r.opaque) all_opaque = false;
+        if (d.identity) {
+            for (uint32_t p = 0; p < ntri; ++p)
+                world_items.push_back(make_uint4((uint32_t)i, d.blas_geo, p, r.opaque ? 1u : 0u));
+        } else {
+            blas_needed[d.blas_geo] = 1;
+            tlas_ids.push_back((uint32_t)i);
+        }
+    }
+    // pool sizes
+    size_t nnodes = 0, ntris = 0;
+    auto add = [&](size_t n) {
+        nnodes += n > 1 ? n - 1 : 0;
+        ntris += n;
+    };
+    add(world_items.size());
+    std::vector<uint32_t> blas_node_base(s->ngeo, 0), blas_tri_base(s->ngeo, 0);
+    for (uint32_t g = 0; g < s->ngeo; ++g) {
+        if (!blas_needed[g]) continue;
+        blas_node_base[g] = (uint32_t)nnodes;
+        blas_tri_base[g] = (uint32_t)ntris;
+        add(s->ranges[g].i_len / 3);
+    }
+    const uint32_t tlas_node_base = (uint32_t)nnodes, tlas_tri_base = (uint32_t)ntris;
+    add(tlas_ids.size());
+    if (ntris >= (1u << 28)) return fail(c, GBRT_E_INVALID, "scene exceeds 2^28 leaf slots");
+    CU(c, s->nodes.alloc(std::max<size_t>(1, nnodes) * sizeof(BNode2)), "cudaMalloc(nodes)");
+    CU(c, s->tris.alloc(std::max<size_t>(1, ntris) * sizeof(TriRec)), "cudaMalloc(tris)");
+    DevScene& v = s->view;
+    v.has_world = 0;
+    v.has_tlas = 0;
+    v.all_opaque = all_opaque ? 1u : 0u;
+    s->all_opaque = all_opaque;
+    // world BVH
+    if (!world_items.empty()) {
+        CU(c, upload(s->items, world_items.data(), world_items.size(), st), "upload(items)");
+        BvhResult r;
+        CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                 s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)world_items.size(),
+                                 s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st),
+           "build world BVH");
+        v.has_world = 1;
+        v.world_root = r.root;
+        v.world_lo = r.lo;
+        v.world_hi = r.hi;
+    }
+    // BLASes + TLAS
+    if (!tlas_ids.empty()) {
+        std::vector<float4> blo(s->ngeo), bhi(s->ngeo);
+        std::vector<int32_t> broot(s->ngeo, 0);
+        DevBuf bitems;
+        for (uint32_t g = 0; g < s->ngeo; ++g) {
+            if (!blas_needed[g]) continue;
+            const uint32_t ntri = s->ranges[g].i_len / 3;
+            std::vector<uint4> items(ntri);
+            for (uint32_t p = 0; p < ntri; ++p) items[p] = make_uint4(0u, g, p, s->ranges[g].opaque ? 1u : 0u);
+            CU(c, upload(bitems, items.data(), items.size(), st), "upload(blas items)");
+            BvhResult r;
+            CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                     s->prims.as<gbrt_priminfo>(), bitems.as<uint4>(), ntri, s->nodes.as<BNode2>(),
+                                     blas_node_base[g], s->tris.as<TriRec>(), blas_tri_base[g], &r, st),
+               "build BLAS");
+            broot[g] = r.root;
+            blo[g] = r.lo;
+            bhi[g] = r.hi;
+        }
+        const uint32_t nt = (uint32_t)tlas_ids.size();
+        std::vector<float4> ilo(nt), ihi(nt);
+        for (uint32_t k = 0; k < nt; ++k) {
+            DevInstance& d = hinst[tlas_ids[k]];
+            d.blas_root = broot[d.blas_geo];
+            d.has_blas = 1;
+            ilo[k] = blo[d.blas_geo];
+            ihi[k] = bhi[d.blas_geo];
+        }
+        CU(c, upload(s->inst, hinst.data(), hinst.size(), st), "upload(instances)");
+        DevBuf d_ids, d_blo, d_bhi, d_lo, d_hi;
+        CU(c, upload(d_ids, tlas_ids.data(), nt, st), "upload(tlas ids)");
+        CU(c, upload(d_blo, ilo.data(), nt, st), "upload");
+        CU(c, upload(d_bhi, ihi.data(), nt, st), "upload");
+        CU(c, d_lo.alloc(nt * sizeof(float4)), "cudaMalloc");
+        CU(c, d_hi.alloc(nt * sizeof(float4)), "cudaMalloc");
+        CU(c, instance_world_boxes(s->inst.as<DevInstance>(), d_ids.as<uint32_t>(), d_blo.as<float4>(),
+                                   d_bhi.as<float4>(), nt, d_lo.as<float4>(), d_hi.as<float4>(), st),
+           "instance boxes");
+        BvhResult r;
+        CU(c, build_instance_bvh(d_lo.as<float4>(), d_hi.as<float4>(), d_ids.as<uint32_t>(), nt,
+                                 s->nodes.as<BNode2>(), tlas_node_base, s->tris.as<TriRec>(), tlas_tri_base, &r, st),
+           "build TLAS");
+        v.has_tlas = 1;
+        v.tlas_root = r.root;
+        v.tlas_lo = r.lo;
+        v.tlas_hi = r.hi;
+        CU(c, cudaStreamSynchronize(st), "sync after TLAS build");
+    } else {
+        CU(c, upload(s->inst, hinst.data(), std::max<size_t>(hinst.size(), 0), st), "upload(instances)");
+        if (hinst.empty()) CU(c, s->inst.alloc(sizeof(DevInstance)), "cudaMalloc");
+        CU(c, cudaStreamSynchronize(st), "sync after build");
+    }
+    refresh_view(s);
+    s->built = v.has_world || v.has_tlas;
+    return GBRT_OK;
+}
+
+void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t launches) {
+    if (!st) return;
+    st->rays_camera = dc.camera;
+    st->rays_extension = dc.extension;
+    st->rays_shadow = dc.shadow;
+    st->rays_total = dc.camera + dc.extension + dc.shadow;
+    st->hits_shaded = dc.shaded;
+    st->device_ms = ms;
+    st->kernel_launches = launches;
+    st->device_status = dc.status;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbrt_version(void) { return "gbrt 0.1 sm_103a"; }
+
+const char* gbrt_last_error(const gbrt_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int gbrt_ctx_create(int device, gbrt_ctx** out) {
+    if (!out) return fail(nullptr, GBRT_E_INVALID, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(nullptr, GBRT_E_NO_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return fail(nullptr, GBRT_E_INVALID, "device index out of range");
+    gbrt_ctx* c = new (std::nothrow) gbrt_ctx();
+    if (!c) return fail(nullptr, GBRT_E_OOM, "host allocation failed");
+    c->device = device;
+    DeviceGuard g(device);
+    auto bail = [&](cudaError_t err, const char* what) {
+        std::string m = std::string(what) + ": " + cudaGetErrorString(err);
+        gbrt_ctx_destroy(c);
+        return fail(nullptr, GBRT_E_CUDA, m);
+    };
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+    if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaEventCreate(&c->tb0)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaEventCreate(&c->tb1)) != cudaSuccess) return bail(e, "event");
+    if ((e = c->counters.alloc(sizeof(DeviceCounters))) != cudaSuccess) return bail(e, "counters");
+    float lut[256];
+    for (int i = 0; i < 256; ++i) {
+        double v = i / 255.0;
+        lut[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+    }
+    if ((e = init_render_constants(lut)) != cudaSuccess) return bail(e, "constants");
+    *out = c;
+    return GBRT_OK;
+}
+
+int gbrt_ctx_destroy(gbrt_ctx* c) {
+    if (!c) return GBRT_OK;
+    {
+        DeviceGuard g(c->device);
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        c->counters.release();
+        c->scratch_rays.release();
+        c->scratch_hits.release();
+        c->scratch_img.release();
+        c->scratch_samples.release();
+        c->scratch_phits.release();
+        if (c->ev0) cudaEventDestroy(c->ev0);
+        if (c->ev1) cudaEventDestroy(c->ev1);
+        if (c->tb0) cudaEventDestroy(c->tb0);
+        if (c->tb1) cudaEventDestroy(c->tb1);
+        if (c->stream) cudaStreamDestroy(c->stream);
+    }
+    delete c;
+    return GBRT_OK;
+}
+
+int gbrt_ctx_mem_info(gbrt_ctx* c, uint64_t* free_b, uint64_t* total_b) {
+    if (!c || !free_b || !total_b) return fail(c, GBRT_E_INVALID, "NULL argument");
+    DeviceGuard g(c->device);
+    size_t f = 0, t = 0;
+    CU(c, cudaMemGetInfo(&f, &t), "cudaMemGetInfo");
+    *free_b = f;
+    *total_b = t;
+    return GBRT_OK;
+}
+
+int gbrt_sync(gbrt_ctx* c) {
+    if (!c) return fail(c, GBRT_E_INVALID, "NULL context");
+    DeviceGuard g(c->device);
+    CU(c, cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return GBRT_OK;
+}
+
+int gbrt_scene_create(gbrt_ctx* c, const gbrt_vertex* v, uint32_t nv, const uint32_t* idx, uint32_t ni,
+                      const gbrt_priminfo* prims, uint32_t ngeo, const gbrt_material_raw* mats, uint32_t nmat,
+                      const gbrt_texture_desc* tex, uint32_t ntex, gbrt_scene** out) {
+    if (!c || !out) return fail(c, GBRT_E_INVALID, "NULL argument");
+    *out = nullptr;
+    if ((nv && !v) || (ni && !idx) || (ngeo && !prims) || (nmat && !mats) || (ntex && !tex))
+        return fail(c, GBRT_E_INVALID, "array pointer is NULL for a non-zero count");
+    if (ni % 3 != 0) return fail(c, GBRT_E_INVALID, "index count is not a multiple of 3");
+    for (uint32_t g = 0; g < ngeo; ++g)
+        if (prims[g].material_id >= nmat)
+            return fail(c, GBRT_E_INVALID, "geometry " + std::to_string(g) + " references a material out of range");
+    DeviceGuard gd(c->device);
+    gbrt_scene* s = new (std::nothrow) gbrt_scene();
+    if (!s) return fail(c, GBRT_E_OOM, "host allocation failed");
+    s->ctx = c;
+    s->nv = nv;
+    s->ni = ni;
+    s->ngeo = ngeo;
+    s->nmat = nmat;
+    s->ntex = ntex;
+    s->h_prims.assign(prims, prims + ngeo);
+    s->h_indices.assign(idx, idx + ni);
+    s->ranges.assign(ngeo, gbrt_geo_range{0, 0, 0, 1});
+    s->has_range.assign(ngeo, 0);
+    cudaStream_t st = c->stream;
+    auto bail = [&](cudaError_t e, const char* what) {
+        delete s;
+        return cuda_fail(c, e, what);
+    };
+    cudaError_t e;
+    if ((e = upload(s->vertices, v, nv, st)) != cudaSuccess) return bail(e, "upload(vertices)");
+    if ((e = upload(s->indices, idx, ni, st)) != cudaSuccess) return bail(e, "upload(indices)");
+    if ((e = upload(s->prims, prims, ngeo, st)) != cudaSuccess) return bail(e, "upload(prims)");
+    if ((e = upload(s->mats, mats, nmat, st)) != cudaSuccess) return bail(e, "upload(materials)");
+    std::vector<DevTexture> dt(ntex);
+    for (uint32_t i = 0; i < ntex; ++i) {
+        const gbrt_texture_desc& t = tex[i];
+        std::memset(&dt[i], 0, sizeof(DevTexture));
+        if (t.format > GBRT_TEX_RGBA16F || t.wrap_s > 2 || t.wrap_t > 2) {
+            delete s;
+            return fail(c, GBRT_E_INVALID, "texture " + std::to_string(i) + ": bad format or wrap mode");
+        }
+        const size_t bytes = (size_t)t.width * t.height * (t.format == GBRT_TEX_RGBA16F ? 8 : 4);
+        DevBuf* b = new DevBuf();
+        s->tex_data.push_back(b);
+        if (bytes && t.data) {
+            if ((e = b->alloc(bytes)) != cudaSuccess) return bail(e, "cudaMalloc(texture)");
+            if ((e = cudaMemcpyAsync(b->p, t.data, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+                return bail(e, "upload(texture)");
+            dt[i].data = b->p;
+            dt[i].w = t.width;
+            dt[i].h = t.height;
+        }
+        dt[i].format = t.format;
+        dt[i].wrap_s = t.wrap_s;
+        dt[i].wrap_t = t.wrap_t;
+    }
+    if ((e = upload(s->tex_descs, dt.data(), dt.size(), st)) != cudaSuccess) return bail(e, "upload(texture descs)");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return bail(e, "sync");
+    refresh_view(s);
+    *out = s;
+    return GBRT_OK;
+}
+
+int gbrt_scene_destroy(gbrt_scene* s) {
+    if (!s) return GBRT_OK;
+    DeviceGuard g(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    delete s;
+    return GBRT_OK;
+}
+
+int gbrt_blas_build(gbrt_scene* s, const gbrt_geo_range* r, uint32_t n, uint32_t flags) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (n && !r) return fail(c, GBRT_E_INVALID, "ranges is NULL");
+    if (flags != 0) return fail(c, GBRT_E_INVALID, "flags must be 0");
+    for (uint32_t i = 0; i < n; ++i) {
+        const gbrt_geo_range& g = r[i];
+        if (g.geo_id >= s->ngeo) return fail(c, GBRT_E_INVALID, "geo_id out of range");
+        if (g.i_len % 3 != 0) return fail(c, GBRT_E_INVALID, "i_len % 3 != 0");  // acceleration_structures.rs:33
+        const gbrt_priminfo& p = s->h_prims[g.geo_id];
+        if ((uint64_t)p.i_offset + g.i_len > s->ni) return fail(c, GBRT_E_INVALID, "index range past the index buffer");
+        if ((uint64_t)p.v_offset + g.v_len > s->nv) return fail(c, GBRT_E_INVALID, "vertex range past the vertex buffer");
+        for (uint32_t k = 0; k < g.i_len; ++k)
+            if (s->h_indices[p.i_offset + k] >= g.v_len)
+                return fail(c, GBRT_E_INVALID, "geometry " + std::to_string(g.geo_id) + ": index " +
+                                                   std::to_string(s->h_indices[p.i_offset + k]) + " >= v_len");
+        s->ranges[g.geo_id] = g;
+        s->has_range[g.geo_id] = 1;
+    }
+    s->built = false;
+    return GBRT_OK;
+}
+
+int gbrt_tlas_build(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
+    if (!s) return GBRT_E_INVALID;
+    if (n && !in) return fail(s->ctx, GBRT_E_INVALID, "instances is NULL");
+    DeviceGuard g(s->ctx->device);
+    s->instances.assign(in, in + n);
+    return build_all(s);
+}
+
+int gbrt_tlas_update(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
+    if (!s) return GBRT_E_INVALID;
+    if (n != s->instances.size()) return fail(s->ctx, GBRT_E_INVALID, "instance count differs from the built TLAS");
+    return gbrt_tlas_build(s, in, n);
+}
+
+int gbrt_skin_and_refit(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (nskin && !skins) return fail(c, GBRT_E_INVALID, "skins is NULL");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS before skinning");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    if (!s->skinned) {  // keep the bind-pose vertices (the reference's vertex_buffer)
+        CU(c, s->base_vertices.alloc(s->vertices.bytes), "cudaMalloc(base vertices)");
+        CU(c, cudaMemcpyAsync(s->base_vertices.p, s->vertices.p, s->vertices.bytes, cudaMemcpyDeviceToDevice, st),
+           "copy");
+        s->skinned = true;
+    }
+    CU(c, upload(s->skins, skins, nskin, st), "upload(skins)");
+    CU(c, launch_skinning(s->base_vertices.as<gbrt_vertex>(), s->vertices.as<gbrt_vertex>(), s->nv,
+                          s->skins.as<gbrt_skin_raw>(), nskin, st),
+       "skinning");
+    return build_all(s);
+}
+
+int gbrt_lights_set(gbrt_scene* s, const gbrt_light_raw* d, uint32_t nd, const gbrt_light_raw* p, uint32_t np) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if ((nd && !d) || (np && !p)) return fail(c, GBRT_E_INVALID, "lights pointer is NULL");
+    DeviceGuard g(c->device);
+    CU(c, upload(s->dlights, d, nd, c->stream), "upload(dlights)");
+    CU(c, upload(s->plights, p, np, c->stream), "upload(plights)");
+    CU(c, cudaStreamSynchronize(c->stream), "sync");
+    s->nd = nd;
+    s->np = np;
+    refresh_view(s);
+    return GBRT_OK;
+}
+
+int gbrt_skybox_set(gbrt_scene* s, uint32_t size, const uint8_t* faces) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    DeviceGuard g(c->device);
+    if (!faces || size == 0) {
+        s->sky.release();
+        s->sky_size = 0;
+    } else {
+        CU(c, upload(s->sky, faces, (size_t)size * size * 4 * 6, c->stream), "upload(skybox)");
+        CU(c, cudaStreamSynchronize(c->stream), "sync");
+        s->sky_size = size;
+    }
+    refresh_view(s);
+    return GBRT_OK;
+}
+
+int gbrt_accum_create(gbrt_ctx* c, uint32_t w, uint32_t h, gbrt_accum** out) {
+    if (!c || !out || w == 0 || h == 0) return fail(c, GBRT_E_INVALID, "bad accumulation size or NULL argument");
+    *out = nullptr;
+    DeviceGuard g(c->device);
+    gbrt_accum* a = new (std::nothrow) gbrt_accum();
+    if (!a) return fail(c, GBRT_E_OOM, "host allocation failed");
+    a->ctx = c;
+    a->w = w;
+    a->h = h;
+    cudaError_t e = a->buf.alloc((size_t)w * h * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->buf.p, 0, a->buf.bytes, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        delete a;
+        return cuda_fail(c, e, "accumulation buffer");
+    }
+    *out = a;
+    return GBRT_OK;
+}
+
+int gbrt_accum_reset(gbrt_accum* a) {
+    if (!a) return GBRT_E_INVALID;
+    DeviceGuard g(a->ctx->device);
+    CU(a->ctx, cudaMemsetAsync(a->buf.p, 0, a->buf.bytes, a->ctx->stream), "memset");
+    return GBRT_OK;
+}
+
+int gbrt_accum_download(gbrt_accum* a, float* dst) {
+    if (!a || !dst) return a ? fail(a->ctx, GBRT_E_INVALID, "dst is NULL") : GBRT_E_INVALID;
+    DeviceGuard g(a->ctx->device);
+    CU(a->ctx, cudaMemcpyAsync(dst, a->buf.p, a->buf.bytes, cudaMemcpyDeviceToHost, a->ctx->stream), "download");
+    CU(a->ctx, cudaStreamSynchronize(a->ctx->stream), "sync");
+    return GBRT_OK;
+}
+
+int gbrt_accum_destroy(gbrt_accum* a) {
+    if (!a) return GBRT_OK;
+    DeviceGuard g(a->ctx->device);
+    cudaStreamSynchronize(a->ctx->stream);
+    delete a;
+    return GBRT_OK;
+}
+
+int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t* out_rgba8, gbrt_stats* stats,
+                   const gbrt_render_opts* opts) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (!ubo || !acc) return fail(c, GBRT_E_INVALID, "ubo or accumulation buffer is NULL");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before rendering");
+    if (acc->ctx != c) return fail(c, GBRT_E_INVALID, "accumulation buffer belongs to another context");
+    if (ubo->number_of_samples == 0 || ubo->total_number_of_samples < ubo->number_of_samples)
+        return fail(c, GBRT_E_INVALID, "need 0 < number_of_samples <= total_number_of_samples");
+    if (opts && opts->mode > GBRT_MODE_WAVEFRONT) return fail(c, GBRT_E_INVALID, "unknown render mode");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const uint32_t W = acc->w, H = acc->h, ns = ubo->number_of_samples;
+    const size_t npix = (size_t)W * H;
+    RenderOut out{};
+    out.width = W;
+    out.height = H;
+    out.accum = acc->buf.as<float4>();
+    out.counters = c->counters.as<DeviceCounters>();
+    if (out_rgba8) {
+        CU(c, c->scratch_img.reserve(npix * 4), "cudaMalloc(image)");
+        out.rgba8 = c->scratch_img.as<uchar4>();
+    }
+    if (opts && opts->sample_radiance) {
+        CU(c, c->scratch_samples.reserve(npix * ns * 3 * sizeof(float)), "cudaMalloc(samples)");
+        out.sample_radiance = c->scratch_samples.as<float>();
+    }
+    if (opts && opts->primary_hits) {
+        CU(c, c->scratch_phits.reserve(npix * ns * sizeof(gbrt_hit)), "cudaMalloc(primary hits)");
+        out.primary_hits = c->scratch_phits.as<gbrt_hit>();
+    }
+    CU(c, cudaMemsetAsync(out.counters, 0, sizeof(DeviceCounters), st), "memset");
+    CU(c, cudaEventRecord(c->ev0, st), "event");
+    CU(c, launch_megakernel(s->view, *ubo, out, st), "megakernel launch");
+    CU(c, cudaEventRecord(c->ev1, st), "event");
+    if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
+    if (out.sample_radiance)
+        CU(c, cudaMemcpyAsync(opts->sample_radiance, out.sample_radiance, npix * ns * 3 * sizeof(float),
+                              cudaMemcpyDeviceToHost, st),
+           "download samples");
+    if (out.primary_hits)
+        CU(c, cudaMemcpyAsync(opts->primary_hits, out.primary_hits, npix * ns * sizeof(gbrt_hit),
+                              cudaMemcpyDeviceToHost, st),
+           "download hits");
+    DeviceCounters dc;
+    CU(c, cudaMemcpyAsync(&dc, out.counters, sizeof(dc), cudaMemcpyDeviceToHost, st), "download counters");
+    CU(c, cudaStreamSynchronize(st), "render");
+    float ms = 0.0f;
+    CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
+    fill_stats(stats, dc, ms, 1);
+    if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit (status " +
+                                                            std::to_string(dc.status) + ")");
+    return GBRT_OK;
+}
+
+int gbrt_render(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t* out_rgba8, gbrt_stats* stats) {
+    return gbrt_render_ex(s, ubo, acc, out_rgba8, stats, nullptr);
+}
+
+int gbrt_trace_rays_device(gbrt_scene* s, const gbrt_ray* d_rays, uint32_t n, uint32_t flags, gbrt_hit* d_hits) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (n && (!d_rays || !d_hits)) return fail(c, GBRT_E_INVALID, "rays or hits is NULL");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tracing");
+    DeviceGuard g(c->device);
+    CU(c, launch_trace_rays(s->view, d_rays, n, flags, d_hits, nullptr, c->stream), "trace launch");
+    return GBRT_OK;
+}
+
+int gbrt_trace_rays(gbrt_scene* s, const gbrt_ray* rays, uint32_t n, uint32_t flags, gbrt_hit* hits,
+                    gbrt_stats* stats) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (n && (!rays || !hits)) return fail(c, GBRT_E_INVALID, "rays or hits is NULL");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tracing");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CU(c, c->scratch_rays.reserve((size_t)std::max(n, 1u) * sizeof(gbrt_ray)), "cudaMalloc(rays)");
+    CU(c, c->scratch_hits.reserve((size_t)std::max(n, 1u) * sizeof(gbrt_hit)), "cudaMalloc(hits)");
+    DeviceCounters* dcnt = c->counters.as<DeviceCounters>();
+    CU(c, cudaMemsetAsync(dcnt, 0, sizeof(DeviceCounters), st), "memset");
+    if (n) CU(c, cudaMemcpyAsync(c->scratch_rays.p, rays, n * sizeof(gbrt_ray), cudaMemcpyHostToDevice, st), "upload rays");
+    CU(c, cudaEventRecord(c->ev0, st), "event");
+    CU(c, launch_trace_rays(s->view, c->scratch_rays.as<gbrt_ray>(), n, flags, c->scratch_hits.as<gbrt_hit>(), dcnt,
+                            st),
+       "trace launch");
+    CU(c, cudaEventRecord(c->ev1, st), "event");
+    if (n) CU(c, cudaMemcpyAsync(hits, c->scratch_hits.p, n * sizeof(gbrt_hit), cudaMemcpyDeviceToHost, st), "download hits");
+    DeviceCounters dc;
+    CU(c, cudaMemcpyAsync(&dc, dcnt, sizeof(dc), cudaMemcpyDeviceToHost, st), "download counters");
+    CU(c, cudaStreamSynchronize(st), "trace");
+    float ms = 0.0f;
+    CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
+    dc.camera = n;
+    fill_stats(stats, dc, ms, n ? 1 : 0);
+    if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit");
+    return GBRT_OK;
+}
+
+int gbrt_device_alloc(gbrt_ctx* c, uint64_t bytes, void** p) {
+    if (!c || !p) return fail(c, GBRT_E_INVALID, "NULL argument");
+    DeviceGuard g(c->device);
+    CU(c, cudaMalloc(p, bytes), "cudaMalloc");
+    return GBRT_OK;
+}
+int gbrt_device_free(gbrt_ctx* c, void* p) {
+    if (!c) return GBRT_E_INVALID;
+    DeviceGuard g(c->device);
+    CU(c, cudaFree(p), "cudaFree");
+    return GBRT_OK;
+}
+int gbrt_memcpy_h2d(gbrt_ctx* c, void* d, const void* h, uint64_t bytes) {
+    if (!c) return GBRT_E_INVALID;
+    DeviceGuard g(c->device);
+    CU(c, cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream), "h2d");
+    CU(c, cudaStreamSynchronize(c->stream), "sync");
+    return GBRT_OK;
+}
+int gbrt_memcpy_d2h(gbrt_ctx* c, void* h, const void* d, uint64_t bytes) {
+    if (!c) return GBRT_E_INVALID;
+    DeviceGuard g(c->device);
+    CU(c, cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    CU(c, cudaStreamSynchronize(c->stream), "sync");
+    return GBRT_OK;
+}
+int gbrt_timer_begin(gbrt_ctx* c) {
+    if (!c) return GBRT_E_INVALID;
+    DeviceGuard g(c->device);
+    CU(c, cudaEventRecord(c->tb0, c->stream), "event");
+    return GBRT_OK;
+}
+int gbrt_timer_end(gbrt_ctx* c, double* ms) {
+    if (!c || !ms) return fail(c, GBRT_E_INVALID, "NULL argument");
+    DeviceGuard g(c->device);
+    CU(c, cudaEventRecord(c->tb1, c->stream), "event");
+    CU(c, cudaEventSynchronize(c->tb1), "event sync");
+    float f = 0;
+    CU(c, cudaEventElapsedTime(&f, c->tb0, c->tb1), "event time");
+    *ms = f;
+    return GBRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+// kernels.h — host-visible launchers of the device code.
+#pragma once
+#include <cuda_runtime.h>
+#include "scene.cuh"
+
+namespace gbrt {
+
+struct DeviceCounters {
+    unsigned long long camera, extension, shadow, shaded, nodes, tris;
+    unsigned int status;
+    unsigned int _pad;
+};
+
+struct RenderOut {
+    uint32_t width, height;
+    float4* accum;             // width*height running sums (required)
+    uchar4* rgba8;             // tone-mapped image, may be null
+    float* sample_radiance;    // [pixel][sample][3], may be null
+    gbrt_hit* primary_hits;    // [pixel][sample], may be null
+    DeviceCounters* counters;  // required
+};
+
+// render.cu
+cudaError_t init_render_constants(const float* srgb_lut);
+cudaError_t launch_megakernel(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, cudaStream_t st);
+cudaError_t launch_trace_rays(const DevScene& s, const gbrt_ray* rays, uint32_t n, uint32_t flags, gbrt_hit* hits,
+                              DeviceCounters* cnt, cudaStream_t st);
+
+// bvh_build.cu -------------------------------------------------------------
+// A BVH over n items is written into the scene pools: inner nodes at
+// nodes[node_base ...], the items' TriRec slots (in leaf order) at
+// tris[tri_base ... tri_base + n).  The root is an inner node index or a
+// leaf code.
+struct BvhResult {
+    int32_t root;
+    float4 lo, hi;  // root bounds
+};
+
+// Item descriptors for triangle BVHs: x = instance id (world BVH) or 0,
+// y = BLAS geometry id, z = primitive id, w = opaque flag.
+cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
+                               const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
+                               uint32_t tri_base, BvhResult* result_host, cudaStream_t st);
+
+// TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
+// the instance ids.
+cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_t* inst_ids, uint32_t n,
+                               BNode2* nodes, uint32_t node_base, TriRec* tris, uint32_t tri_base,
+                               BvhResult* result_host, cudaStream_t st);
+
+// Refit: recomputes every inner-node box of a triangle BVH bottom-up from the
+// current vertex positions, keeping the topology (used after skinning).
+cudaError_t refit_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
+                               BNode2* nodes, uint32_t node_base, uint32_t num_inner, TriRec* tris,
+                               uint32_t tri_base, uint32_t n, const int32_t* parents, int32_t root,
+                               BvhResult* result_host, cudaStream_t st);
+
+// World boxes of transformed instances from their BLAS root bounds.
+cudaError_t instance_world_boxes(const DevInstance* inst, const uint32_t* ids, const float4* blas_lo,
+                                 const float4* blas_hi, uint32_t n, float4* lo, float4* hi, cudaStream_t st);
+
+// skin.cu
+cudaError_t launch_skinning(const gbrt_vertex* vin, gbrt_vertex* vout, uint32_t nv, const gbrt_skin_raw* skins,
+                            uint32_t nskin, cudaStream_t st);
+
+}  // namespace gbrt

@@ -1,0 +1,263 @@
+"""ctypes binding of libgbrt.so (include/gbrt.h) and a thin host layer that
+mirrors the reference's render-frame API.
+
+The reference's per-frame path (crates/examples/gltf_viewer/src/main.rs) is:
+``create_as`` (BLAS per geometry + TLAS, acceleration_structures.rs:79-129),
+``create_top_as`` (TLAS only, :136-249), a UBO upload and ``trace_rays``
+(main.rs:215-270) into an accumulation image.  :class:`Renderer` exposes the
+same steps (``create_as``, ``create_top_as``, ``update_lights``,
+``render``) on top of the C ABI.  Failures raise :class:`GbrtError` carrying
+the library's status code and message (the reference panics/propagates
+``anyhow`` errors instead).
+
+There is no CPU fallback: if libgbrt.so or a CUDA device is missing, calls
+raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import types as T
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgbrt.so")
+
+OK, E_INVALID, E_CUDA, E_OOM, E_DEVICE_LIMIT, E_NOT_BUILT, E_NO_DEVICE, E_BUSY = 0, -1, -2, -3, -4, -5, -6, -7
+MODE_AUTO, MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1, 2
+
+# name -> (restype, argtypes); every symbol include/gbrt.h declares
+P, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+SIGNATURES = {
+    "gbrt_version": (C.c_char_p, []),
+    "gbrt_last_error": (C.c_char_p, [P]),
+    "gbrt_ctx_create": (i32, [i32, C.POINTER(P)]),
+    "gbrt_ctx_destroy": (i32, [P]),
+    "gbrt_ctx_mem_info": (i32, [P, C.POINTER(u64), C.POINTER(u64)]),
+    "gbrt_sync": (i32, [P]),
+    "gbrt_scene_create": (i32, [P, P, u32, P, u32, P, u32, P, u32, P, u32, C.POINTER(P)]),
+    "gbrt_scene_destroy": (i32, [P]),
+    "gbrt_blas_build": (i32, [P, P, u32, u32]),
+    "gbrt_tlas_build": (i32, [P, P, u32]),
+    "gbrt_tlas_update": (i32, [P, P, u32]),
+    "gbrt_skin_and_refit": (i32, [P, P, u32]),
+    "gbrt_lights_set": (i32, [P, P, u32, P, u32]),
+    "gbrt_skybox_set": (i32, [P, u32, P]),
+    "gbrt_accum_create": (i32, [P, u32, u32, C.POINTER(P)]),
+    "gbrt_accum_reset": (i32, [P]),
+    "gbrt_accum_download": (i32, [P, P]),
+    "gbrt_accum_destroy": (i32, [P]),
+    "gbrt_render": (i32, [P, P, P, P, P]),
+    "gbrt_render_ex": (i32, [P, P, P, P, P, P]),
+    "gbrt_trace_rays": (i32, [P, P, u32, u32, P, P]),
+    "gbrt_trace_rays_device": (i32, [P, P, u32, u32, P]),
+    "gbrt_device_alloc": (i32, [P, u64, C.POINTER(P)]),
+    "gbrt_device_free": (i32, [P, P]),
+    "gbrt_memcpy_h2d": (i32, [P, P, P, u64]),
+    "gbrt_memcpy_d2h": (i32, [P, P, P, u64]),
+    "gbrt_timer_begin": (i32, [P]),
+    "gbrt_timer_end": (i32, [P, C.POINTER(C.c_double)]),
+}
+
+
+class GbrtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbrt error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Loads libgbrt.so (building it first if absent) and binds SIGNATURES."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            from . import build
+            build.build()
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class TexDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32), ("wrap_s", C.c_uint32),
+                ("wrap_t", C.c_uint32), ("_pad", C.c_uint32), ("data", C.c_void_p)]
+
+
+class RenderOpts(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("flags", C.c_uint32), ("sample_radiance", C.c_void_p),
+                ("primary_hits", C.c_void_p)]
+
+
+class Context:
+    """gbrt_ctx: one CUDA device + stream."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = P()
+        rc = self.L.gbrt_ctx_create(device, C.byref(h))
+        if rc != OK:
+            raise GbrtError(rc, self.L.gbrt_last_error(None).decode())
+        self.h = h
+
+    def check(self, rc):
+        if rc != OK:
+            raise GbrtError(rc, self.L.gbrt_last_error(self.h).decode())
+
+    def mem_info(self):
+        f, t = u64(), u64()
+        self.check(self.L.gbrt_ctx_mem_info(self.h, C.byref(f), C.byref(t)))
+        return f.value, t.value
+
+    def sync(self):
+        self.check(self.L.gbrt_sync(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gbrt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Accum:
+    """gbrt_accum: device RGBA32F running sum (the reference's acc_image)."""
+
+    def __init__(self, ctx, width, height):
+        self.ctx, self.w, self.h_ = ctx, width, height
+        h = P()
+        ctx.check(ctx.L.gbrt_accum_create(ctx.h, width, height, C.byref(h)))
+        self.h = h
+
+    def reset(self):
+        self.ctx.check(self.ctx.L.gbrt_accum_reset(self.h))
+
+    def download(self):
+        out = np.zeros((self.h_, self.w, 4), np.float32)
+        self.ctx.check(self.ctx.L.gbrt_accum_download(self.h, _p(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.gbrt_accum_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Scene:
+    """gbrt_scene created from a scenes.SceneData (the reference's Buffers +
+    textures), with create_as / create_top_as like
+    crates/libs/asset_loader/src/acceleration_structures.rs."""
+
+    def __init__(self, ctx, sd, build=True):
+        self.ctx, self.sd = ctx, sd
+        L = ctx.L
+        descs = (TexDesc * max(1, len(sd.textures)))()
+        self._keep = []
+        for i, (w, h, fmt, ws, wt, data) in enumerate(sd.textures):
+            data = np.ascontiguousarray(data)
+            self._keep.append(data)
+            descs[i] = TexDesc(w, h, fmt, ws, wt, 0, data.ctypes.data)
+        h = P()
+        ctx.check(L.gbrt_scene_create(ctx.h, _p(sd.vertices), len(sd.vertices), _p(sd.indices), len(sd.indices),
+                                      _p(sd.prims), len(sd.prims), _p(sd.materials), len(sd.materials),
+                                      C.cast(descs, P), len(sd.textures), C.byref(h)))
+        self.h = h
+        if build:
+            self.create_as()
+            self.update_lights(sd.dlights, sd.plights)
+            if sd.skybox is not None:
+                self.set_skybox(*sd.skybox)
+
+    def create_as(self, ranges=None, instances=None):
+        """BLAS per geometry, then the TLAS (create_as, acceleration_structures.rs:79-129)."""
+        ranges = self.sd.geo_ranges if ranges is None else ranges
+        self.ctx.check(self.ctx.L.gbrt_blas_build(self.h, _p(ranges), len(ranges), 0))
+        self.create_top_as(instances)
+
+    def create_top_as(self, instances=None):
+        """TLAS only (create_top_as, acceleration_structures.rs:136-249)."""
+        inst = self.sd.instances if instances is None else np.ascontiguousarray(instances, T.INSTANCE)
+        self.ctx.check(self.ctx.L.gbrt_tlas_build(self.h, _p(inst), len(inst)))
+
+    def update_tlas(self, instances):
+        inst = np.ascontiguousarray(instances, T.INSTANCE)
+        self.ctx.check(self.ctx.L.gbrt_tlas_update(self.h, _p(inst), len(inst)))
+
+    def skin_and_refit(self, skins):
+        skins = np.ascontiguousarray(skins, T.SKIN)
+        self.ctx.check(self.ctx.L.gbrt_skin_and_refit(self.h, _p(skins), len(skins)))
+
+    def update_lights(self, dlights, plights):
+        d = np.ascontiguousarray(dlights, T.LIGHT)
+        p = np.ascontiguousarray(plights, T.LIGHT)
+        self.ctx.check(self.ctx.L.gbrt_lights_set(self.h, _p(d), len(d), _p(p), len(p)))
+
+    def set_skybox(self, size, faces):
+        faces = None if faces is None else np.ascontiguousarray(faces, np.uint8)
+        self.ctx.check(self.ctx.L.gbrt_skybox_set(self.h, size, _p(faces)))
+
+    def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False):
+        """One frame (record_raytracing_commands + the shaders).  Returns a dict
+        with 'image' (HxWx4 uint8 or None), 'stats', and the optional
+        per-sample radiance [pixel][sample][3] and primary hits."""
+        ubo = np.asarray(ubo, T.UBO).reshape(())
+        W, H = accum.w, accum.h_
+        ns = int(ubo["number_of_samples"])
+        img = np.zeros((H, W, 4), np.uint8) if image else None
+        st = np.zeros((), T.STATS)
+        samples = np.zeros((H * W, ns, 3), np.float32) if want_samples else None
+        hits = np.zeros((H * W, ns), T.HIT) if want_hits else None
+        opts = RenderOpts(mode, 0, samples.ctypes.data if want_samples else None,
+                          hits.ctypes.data if want_hits else None)
+        self.ctx.check(self.ctx.L.gbrt_render_ex(self.h, _p(ubo), accum.h, _p(img), _p(st), C.byref(opts)))
+        return dict(image=img, stats=st, samples=samples, hits=hits)
+
+    def trace(self, rays, flags=0):
+        rays = np.ascontiguousarray(rays, T.RAY)
+        hits = np.zeros(len(rays), T.HIT)
+        st = np.zeros((), T.STATS)
+        self.ctx.check(self.ctx.L.gbrt_trace_rays(self.h, _p(rays), len(rays), flags, _p(hits), _p(st)))
+        return hits, st
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.gbrt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Renderer:
+    """The reference's GltfViewer render-frame loop on the C ABI: owns a
+    scene and an accumulation buffer and accumulates samples frame after
+    frame (main.rs:189-270; reset on change, main.rs:336-353)."""
+
+    def __init__(self, ctx, sd, width, height):
+        self.ctx, self.sd = ctx, sd
+        self.scene = Scene(ctx, sd)
+        self.accum = Accum(ctx, width, height)
+        self.width, self.height = width, height
+        self.total_number_of_samples = 0
+
+    def reset_samples(self):
+        self.total_number_of_samples = 0
+        self.accum.reset()
+
+    def frame(self, samples=3, **ubo_kw):
+        self.total_number_of_samples += samples
+        ubo = self.sd.ubo(self.width, self.height, samples=samples, total=self.total_number_of_samples, **ubo_kw)
+        return self.scene.render(ubo, self.accum)

@@ -1,0 +1,266 @@
+"""CPU checks of the oracle: known-answer vectors of the shader library,
+analytic hits, watertightness, and regression against the golden fixtures.
+
+The oracle is the reference for every GPU parity test; its parity with the
+reference shaders is unpinned (no runnable reference and no golden vectors
+upstream), so these tests pin it against independent restatements and
+analytic answers instead.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle as O
+from rustracer_gb300 import scenes, types as T
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_rng_known_answers():
+    """Random.glsl: TEA, LCG RandomFloat, pcg4d, rand vs the independent
+    pure-Python restatement that generated golden_rng.json."""
+    g = json.load(open(os.path.join(GOLDEN, "golden_rng.json")))
+    for a, b, v in g["tea"]:
+        assert O.tea(a, b) == v
+    for vin, vout in g["pcg4d"]:
+        assert list(O.pcg4d(vin)) == vout
+    for s, seq in g["rand"]:
+        assert np.array_equal(O.rand_sequence(s, 8)[0], np.float32(seq))
+    for s, seq in g["lcg"]:
+        assert np.array_equal(O.random_float_sequence(s, 8), np.float32(seq))
+
+
+def test_rng_python_restatement_consistent():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    rng = np.random.default_rng(1)
+    for _ in range(50):
+        a, b = (int(x) for x in rng.integers(0, 2**32, 2))
+        assert O.tea(a, b) == mg.tea(a, b)
+        v = [int(x) for x in rng.integers(0, 2**32, 4)]
+        assert list(O.pcg4d(v)) == mg.pcg4d(v)
+
+
+def _np_tonemap(mode, c):
+    c = np.asarray(c, np.float64)
+    if mode == 0:
+        return (c / (c + 1)) ** (1 / 2.2)
+    if mode == 3:
+        return np.clip((c * (2.51 * c + 0.03)) / (c * (2.43 * c + 0.59) + 0.14), 0, 1) ** (1 / 2.2)
+    if mode == 2:
+        c = np.maximum(0, c - 0.004)
+        return (c * (6.2 * c + 0.5)) / (c * (6.2 * c + 1.7) + 0.06)
+    if mode == 4:
+        return c ** (1 / 2.2)
+    u = lambda x: ((x * (0.15 * x + 0.05) + 0.004) / (x * (0.15 * x + 0.5) + 0.06)) - 0.02 / 0.3
+    return (u(c * 2) / u(np.float64(11.2))) ** (1 / 2.2)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+def test_tonemap_formulas(mode):
+    """Tonemapping.glsl operators vs a float64 numpy restatement."""
+    for c in ([0.0, 0.5, 1.0], [0.01, 2.0, 10.0], [100.0, 0.25, 3.0]):
+        assert np.allclose(O.tonemap(mode, c), _np_tonemap(mode, c), rtol=2e-5, atol=5e-4)
+
+
+def _np_brdf(N, L, V, base, metallic, rough, ior=1.5):
+    """PBR.glsl evalCombinedBRDF in float64 (GGX D, height-correlated
+    Smith G2, Schlick F with shadowed F90, Frostbite diffuse)."""
+    N, L, V, base = (np.asarray(x, np.float64) for x in (N, L, V, base))
+    lum = lambda c: c @ [0.2126, 0.7152, 0.0722]
+    f = (ior - 1) / (ior + 1)
+    dF0 = np.minimum(f * f * np.ones(3), 1.0)
+    F0 = dF0 * (1 - metallic) + base * metallic
+    F90 = np.ones(3)
+    cdiff = base * (1 - metallic)
+    H = (L + V) / np.linalg.norm(L + V)
+    NL, NV = N @ L, N @ V
+    if NL <= 0 or NV <= 0:
+        return np.zeros(3)
+    NL, NV = min(max(1e-5, NL), 1), min(max(1e-5, NV), 1)
+    LH, NH, VH = (min(max(x, 0), 1) for x in (L @ H, N @ H, V @ H))
+    a = rough * rough
+    a2 = a * a
+    F = F0 + (min(1, lum(F90)) - F0) * (1 - VH) ** 5
+    b = (max(1e-5, a2) - 1) * NH * NH + 1
+    D = max(1e-5, a2) / (3.141592653589 * b * b)
+    ga = lambda s: s / (max(1e-5, a) * math.sqrt(1 - min(0.99999, s * s)))
+    lam = lambda x: (-1 + math.sqrt(1 + 1 / (x * x))) * 0.5
+    G2 = 1 / (1 + lam(ga(NL)) + lam(ga(NV)))
+    spec = F * G2 * D / (4 * NL * NV) * NL
+    fd90 = 0.5 * rough + 2 * LH * LH * rough - 1
+    fdiff = (1 + fd90 * (1 - NL) ** 5) * (1 + fd90 * (1 - NV) ** 5) * (1 * (1 - rough) + rough / 1.51)
+    return cdiff * fdiff / 3.141592653589 * NL + spec
+
+
+def test_brdf_vs_float64_restatement():
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        N = np.array([0, 0, 1.0])
+        L, V = rng.normal(size=3), rng.normal(size=3)
+        L[2], V[2] = abs(L[2]) + 0.05, abs(V[2]) + 0.05
+        L, V = L / np.linalg.norm(L), V / np.linalg.norm(V)
+        base = rng.uniform(0.1, 0.9, 3)
+        m, r = float(rng.random() < 0.3), rng.uniform(0.05, 1.0)
+        got = O.eval_combined_brdf(N, L, V, base, m, r)
+        want = _np_brdf(N, L, V, base, m, r)
+        assert np.allclose(got, want, rtol=2e-3, atol=1e-6), (got, want)
+
+
+def test_brdf_backfacing_is_zero():
+    z = O.eval_combined_brdf([0, 0, 1], [0, 0.6, -0.8], [0, 0, 1], [0.5] * 3, 0.0, 0.5)
+    assert np.all(z == 0)
+
+
+def test_offset_ray_moves_along_normal():
+    p = np.array([1.5, -2.0, 0.01], np.float32)
+    n = np.array([0.0, 0.0, -1.0], np.float32)
+    q = O.offset_ray(p, n)
+    assert q[0] == p[0] and q[1] == p[1] and q[2] < p[2]
+
+
+def _one_triangle_scene(p0, p1, p2):
+    b = scenes.GeoBuilder()
+    m = b.add_material(scenes.lambert((0.5, 0.5, 0.5)))
+    b.add_mesh(np.array([p0, p1, p2], np.float32), np.array([[0, 1, 2]]), m)
+    return b.finish()
+
+
+def test_single_triangle_analytic_hit():
+    sd = _one_triangle_scene((0, 0, 0), (1, 0, 0), (0, 1, 0))
+    o = O.OracleScene(sd)
+    rays = np.zeros(4, T.RAY)
+    rays["org"] = [(0.25, 0.5, 2.0), (0.25, 0.5, -3.0), (0.7, 0.7, 1.0), (0.1, 0.1, 1.0)]
+    rays["dir"] = [(0, 0, -1), (0, 0, 1), (0, 0, -1), (0, 0, -1)]
+    rays["tmin"], rays["tmax"] = 0.0, 100.0
+    rays["tmax"][3] = 0.5
+    h, _ = o.trace(rays)
+    assert h["t"][0] == 2.0 and h["u"][0] == 0.25 and h["v"][0] == 0.5
+    assert h["t"][1] == 3.0 and h["primitive_id"][1] == 0       # back face: no culling
+    assert h["instance_id"][2] == 0xFFFFFFFF                     # outside
+    assert h["instance_id"][3] == 0xFFFFFFFF                     # beyond tmax
+
+
+def test_watertight_fan():
+    """Rays aimed exactly at the shared edges and the shared vertex of a
+    triangle fan never fall through (Woop et al. 2013)."""
+    k = 12
+    ang = np.linspace(0, 2 * np.pi, k, endpoint=False)
+    pts = np.concatenate([[[0.1, 0.2, 0.0]], np.stack([np.cos(ang), np.sin(ang), 0.3 * np.sin(3 * ang)], 1)])
+    tris = np.array([[0, 1 + i, 1 + (i + 1) % k] for i in range(k)])
+    b = scenes.GeoBuilder()
+    m = b.add_material(scenes.lambert((0.5, 0.5, 0.5)))
+    b.add_mesh(pts.astype(np.float32), tris, m)
+    o = O.OracleScene(b.finish())
+    targets = []
+    for i in range(k):  # points along each spoke, and the hub
+        for s in np.linspace(0, 1, 33)[:-1]:
+            targets.append(pts[0] + s * (pts[1 + i] - pts[0]))
+    targets = np.array(targets, np.float32)
+    rng = np.random.default_rng(0)
+    orgs = targets + np.array([0.0, 0.0, 2.0]) + rng.normal(0, 0.3, targets.shape) * [1, 1, 0]
+    rays = np.zeros(len(targets), T.RAY)
+    rays["org"] = orgs
+    d = targets - orgs
+    rays["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"], rays["tmax"] = 0.0, 100.0
+    h, _ = o.trace(rays)
+    assert np.all(h["instance_id"] == 0), f"{(h['instance_id'] != 0).sum()} rays fell through"
+
+
+def test_fp32_vs_fp64_hits_agree():
+    sd = scenes.random_soup(3000, seed=4)
+    rays = scenes.random_rays(5000, seed=5)
+    o = O.OracleScene(sd)
+    a, _ = o.trace(rays)
+    b, _ = o.trace(rays, fp64=True)
+    same = (a["instance_id"] == b["instance_id"]) & (a["primitive_id"] == b["primitive_id"])
+    assert same.mean() > 0.999
+    hit = a["instance_id"] != 0xFFFFFFFF
+    assert np.allclose(a["t"][hit & same], b["t"][hit & same], rtol=1e-5)
+
+
+def test_bvh_matches_brute_force():
+    """Closest hits through the BVH equal an exhaustive test of every
+    triangle (numpy float64 Moller-Trumbore, away from ties)."""
+    sd = scenes.random_soup(400, seed=9, size=0.1)
+    rays = scenes.random_rays(2000, seed=10)
+    h, _ = O.OracleScene(sd).trace(rays)
+    v = sd.vertices["pos"][:, :3].astype(np.float64)
+    tri = v[sd.indices.reshape(-1, 3)]
+    o, d = rays["org"].astype(np.float64), rays["dir"].astype(np.float64)
+    e1, e2 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]
+    best = np.full(len(rays), np.inf)
+    for j in range(len(tri)):
+        pv = np.cross(d, e2[j])
+        det = pv @ e1[j]
+        tv = o - tri[j, 0]
+        u = np.einsum("ij,ij->i", tv, pv) / det
+        qv = np.cross(tv, e1[j])
+        vv = np.einsum("ij,ij->i", d, qv) / det
+        t = (qv @ e2[j]) / det
+        ok = (u >= 0) & (vv >= 0) & (u + vv <= 1) & (t >= 0)
+        best = np.where(ok & (t < best), t, best)
+    hit = h["instance_id"] != 0xFFFFFFFF
+    assert np.array_equal(hit, np.isfinite(best))
+    assert np.allclose(h["t"][hit], best[hit], rtol=1e-5)
+
+
+def test_cornell_triangle_count_and_layout():
+    sd = scenes.cornell()
+    assert sd.num_triangles == 34
+    assert sd.vertices.dtype.itemsize == 128 and sd.materials.dtype.itemsize == 256
+    assert len(sd.plights) == 0 and len(sd.dlights) == 1 and sd.dlights[0]["intensity"] == 0
+
+
+@pytest.mark.parametrize("k", [0, 1, 3])
+def test_icosphere_counts(k):
+    sd = scenes.icosphere_scene(subdiv=k)
+    assert sd.num_triangles == 34 + 20 * 4 ** k
+
+
+@pytest.mark.parametrize("name", ["golden_cornell_32", "golden_ico2"])
+def test_golden_render_regression(name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ubo = np.frombuffer(g["ubo"].tobytes(), T.UBO)[0]
+    sd = scenes.cornell() if name == "golden_cornell_32" else scenes.icosphere_scene(subdiv=2)
+    w = {"golden_cornell_32": (32, 32), "golden_ico2": (24, 16)}[name]
+    r = O.OracleScene(sd).render(ubo, *w, want_samples=True, want_hits=True, threads=1)
+    assert np.array_equal(r["samples"].view(np.uint32), g["samples"].view(np.uint32))
+    assert np.array_equal(r["hits"], g["hits"])
+    assert np.array_equal(r["image"], g["image"])
+
+
+def test_golden_trace_regression():
+    g = np.load(os.path.join(GOLDEN, "golden_trace_soup.npz"))
+    h, _ = O.OracleScene(scenes.random_soup(500, seed=7)).trace(g["rays"], threads=1)
+    assert np.array_equal(h, g["hits"])
+
+
+def test_render_determinism_across_threads():
+    sd = scenes.icosphere_scene(subdiv=2)
+    ubo = sd.ubo(32, 24, samples=2, bounces=6, exposure=1.0)
+    o = O.OracleScene(sd)
+    a = o.render(ubo, 32, 24, want_samples=True, threads=1)["samples"]
+    b = o.render(ubo, 32, 24, want_samples=True, threads=4)["samples"]
+    assert np.array_equal(a, b)
+
+
+def test_accumulation_semantics():
+    """rgen:132-135: the accumulation image holds the running sum; a frame
+    with NumberOfSamples == TotalNumberOfSamples overwrites it."""
+    sd = scenes.cornell()
+    o = O.OracleScene(sd)
+    acc = np.zeros((16, 16, 4), np.float32)
+    o.render(sd.ubo(16, 16, samples=2, total=2, bounces=4), 16, 16, accum=acc)
+    first = acc.copy()
+    o.render(sd.ubo(16, 16, samples=2, total=4, bounces=4), 16, 16, accum=acc)
+    acc2 = np.zeros((16, 16, 4), np.float32)
+    o.render(sd.ubo(16, 16, samples=4, total=4, bounces=4), 16, 16, accum=acc2)
+    assert np.allclose(acc, acc2, rtol=1e-5, atol=1e-7)
+    assert not np.array_equal(first, acc)
