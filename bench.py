@@ -292,7 +292,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbrt", choices=["gbrt", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
+    ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
+    ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")
     args = ap.parse_args()
+    global W, H, SPP, WORKLOAD
+    if args.res:
+        W, H = (int(x) for x in args.res.lower().split("x"))
+    if args.spp:
+        SPP = args.spp
+    WORKLOAD = f"icosphere{SUBDIV}_cornell_{W}x{H}_{SPP}spp_depth{DEPTH}"
     if args.impl == "reference":
         run_reference(args)
     else:

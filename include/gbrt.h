@@ -378,6 +378,41 @@ int gbrt_trace_rays_device(gbrt_scene* scene, const gbrt_ray* d_rays, uint32_t n
                            uint32_t ray_flags, gbrt_hit* d_hits);
 
 /* ------------------------------------------------------------------------ */
+/* Allocation-free world-BVH rebuild                                        */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference (it has no API of this kind).
+ *
+ * Rebuilds the merged world BVH of an already built scene, in place, without
+ * allocating or freeing any device memory.  It exists for callers that must
+ * not allocate while they run: a frame loop that rebuilds the BVH of a
+ * deforming mesh every frame (cudaMalloc/cudaFree can synchronise the device
+ * and stall the frame), a host whose device memory is owned by another
+ * allocator or budget, or code that must not fail with out-of-memory half way
+ * through a frame.
+ *
+ * d_vertices: NULL to rebuild from the scene's current vertices, or device
+ * memory holding the scene's full vertex array (nv gbrt_vertex, same layout
+ * and count as at gbrt_scene_create), which replaces the scene's vertices
+ * first.  Indices, geometries and instances stay as built.
+ *
+ * Limits and rules:
+ *  - at most GBRT_NOALLOC_MAX_TRIANGLES triangles in the world BVH; larger
+ *    scenes get GBRT_E_INVALID with a message;
+ *  - every instance must have an identity transform (scenes with transformed
+ *    instances get GBRT_E_INVALID);
+ *  - the build scratch is one static device array of 12 MiB, held by every
+ *    GPU that loads the library until the process exits;
+ *  - the first call on a device looks up that array's device address; make
+ *    that first call before any CUDA stream capture;
+ *  - all calls on a device share the array: calls from one context are
+ *    ordered by its stream, but calls that overlap on the GPU (two contexts
+ *    or threads on the same device at once) race and corrupt each other.
+ * Synchronous: returns after the rebuild has finished. */
+#define GBRT_NOALLOC_MAX_TRIANGLES 65536u
+int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices);
+
+/* ------------------------------------------------------------------------ */
 /* Device memory helpers (for callers without a CUDA runtime of their own)  */
 /* ------------------------------------------------------------------------ */
 int gbrt_device_alloc(gbrt_ctx* ctx, uint64_t bytes, void** d_ptr);

@@ -756,3 +756,78 @@ int gbrt_timer_end(gbrt_ctx* c, double* ms) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free world-BVH rebuild.
+//
+// For callers that must not allocate device memory while they run: a frame
+// loop that rebuilds the BVH of a deforming mesh every frame (cudaMalloc and
+// cudaFree can synchronise the whole device and stall the frame), a host whose
+// device memory belongs to another allocator or budget (a Vulkan or engine
+// heap, a serving process under a hard memory cap), or code that cannot
+// afford to fail with out-of-memory half way through a frame.  The build's
+// scratch (Morton keys, radix tree, subtree boxes, sort temporary storage) lives
+// in the file-scope array below, which every GPU that loads the library keeps
+// until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoallocMaxTriangles = GBRT_NOALLOC_MAX_TRIANGLES;
+constexpr size_t kNoallocScratchBytes = size_t(12) << 20;  // 12 MiB, checked against the layout at set-up
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Once per device, with that device current: the device address of the
+// scratch array (the host-side name of the array is not a device address).
+int noalloc_setup(gbrt_ctx* c, void** out) {
+    if (c->device < 0 || c->device >= kMaxDevices) return fail(c, GBRT_E_INVALID, "device index too large");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[c->device]) {
+        if (bvh_scratch_bytes(kNoallocMaxTriangles) > kNoallocScratchBytes)
+            return fail(c, GBRT_E_INVALID, "static build scratch is smaller than the build layout needs");
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaGetSymbolAddress(build scratch)");
+        g_noalloc_ptr[c->device] = p;
+    }
+    *out = g_noalloc_ptr[c->device];
+    return GBRT_OK;
+}
+
+}  // namespace
+
+extern "C" int gbrt_scene_rebuild_noalloc(gbrt_scene* s, const gbrt_vertex* d_vertices) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS with gbrt_tlas_build before rebuilding");
+    if (s->view.has_tlas)
+        return fail(c, GBRT_E_INVALID,
+                    "the allocation-free rebuild covers scenes whose instances all have identity transforms");
+    if (!s->view.has_world) return fail(c, GBRT_E_NOT_BUILT, "the scene has no world BVH");
+    const size_t n = s->items.bytes / sizeof(uint4);
+    if (n > kNoallocMaxTriangles)
+        return fail(c, GBRT_E_INVALID, "world BVH has " + std::to_string(n) + " triangles; the allocation-free " +
+                                           "rebuild handles at most " + std::to_string(kNoallocMaxTriangles));
+    DeviceGuard g(c->device);
+    void* base = nullptr;
+    int rc = noalloc_setup(c, &base);
+    if (rc != GBRT_OK) return rc;
+    cudaStream_t st = c->stream;
+    if (d_vertices)
+        CU(c, cudaMemcpyAsync(s->vertices.p, d_vertices, s->vertices.bytes, cudaMemcpyDeviceToDevice, st),
+           "copy vertices");
+    const BuildScratch scratch = bvh_scratch_carve(base, kNoallocMaxTriangles);
+    BvhResult r;
+    CU(c, build_triangle_bvh_scratch(scratch, s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                     s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)n,
+                                     s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st),
+       "allocation-free BVH rebuild");
+    CU(c, cudaStreamSynchronize(st), "sync after rebuild");
+    s->view.world_root = r.root;
+    s->view.world_lo = r.lo;
+    s->view.world_hi = r.hi;
+    return GBRT_OK;
+}

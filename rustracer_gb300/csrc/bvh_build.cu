@@ -422,6 +422,98 @@ cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_
     return e;
 }
 
+size_t bvh_sort_temp_bytes(uint32_t n) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, 30);
+    return bytes;
+}
+
+namespace {
+inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+}  // namespace
+
+size_t bvh_scratch_bytes(uint32_t cap) {
+    const size_t n = cap, m = cap > 1 ? cap - 1 : 1;
+    return 4 * al256(n * sizeof(float4)) + 4 * al256(n * sizeof(uint32_t)) + 2 * al256(m * sizeof(uint32_t)) +
+           2 * al256(m * sizeof(uint32_t)) + al256(32) + 4 * al256(n * sizeof(int32_t)) +
+           al256(m * sizeof(float)) + al256(n * sizeof(TriRec)) + al256(bvh_sort_temp_bytes(cap));
+}
+
+BuildScratch bvh_scratch_carve(void* base, uint32_t cap) {
+    const size_t n = cap, m = cap > 1 ? cap - 1 : 1;
+    char* p = static_cast<char*>(base);
+    auto take = [&](size_t bytes) {
+        void* r = p;
+        p += al256(bytes);
+        return r;
+    };
+    BuildScratch s;
+    s.capacity = cap;
+    s.lo = (float4*)take(n * sizeof(float4));
+    s.hi = (float4*)take(n * sizeof(float4));
+    s.ilo = (float4*)take(n * sizeof(float4));
+    s.ihi = (float4*)take(n * sizeof(float4));
+    s.morton_in = (uint32_t*)take(n * sizeof(uint32_t));
+    s.morton = (uint32_t*)take(n * sizeof(uint32_t));
+    s.idx_in = (uint32_t*)take(n * sizeof(uint32_t));
+    s.idx = (uint32_t*)take(n * sizeof(uint32_t));
+    s.range_lo = (uint32_t*)take(m * sizeof(uint32_t));
+    s.range_hi = (uint32_t*)take(m * sizeof(uint32_t));
+    s.collapse = (uint32_t*)take(m * sizeof(uint32_t));
+    s.arrive = (uint32_t*)take(m * sizeof(uint32_t));
+    s.cbounds = (uint32_t*)take(32);
+    s.left = (int32_t*)take(n * sizeof(int32_t));
+    s.right = (int32_t*)take(n * sizeof(int32_t));
+    s.parent_i = (int32_t*)take(n * sizeof(int32_t));
+    s.parent_l = (int32_t*)take(n * sizeof(int32_t));
+    s.cost = (float*)take(m * sizeof(float));
+    s.unsorted = (TriRec*)take(n * sizeof(TriRec));
+    s.sort_tmp_bytes = bvh_sort_temp_bytes(cap);
+    s.sort_tmp = take(s.sort_tmp_bytes);
+    return s;
+}
+
+cudaError_t build_triangle_bvh_scratch(const BuildScratch& bs, const gbrt_vertex* vertices, const uint32_t* indices,
+                                       const gbrt_priminfo* prims, const uint4* items, uint32_t n, BNode2* nodes,
+                                       uint32_t node_base, TriRec* tris, uint32_t tri_base, BvhResult* res,
+                                       cudaStream_t st) {
+    if (n == 0 || n > bs.capacity) return cudaErrorInvalidValue;
+    Scratch s;
+    std::memset(&s, 0, sizeof(s));
+    s.lo = bs.lo;
+    s.hi = bs.hi;
+    s.morton_in = bs.morton_in;
+    s.morton = bs.morton;
+    s.idx_in = bs.idx_in;
+    s.idx = bs.idx;
+    s.left = bs.left;
+    s.right = bs.right;
+    s.parent_i = bs.parent_i;
+    s.parent_l = bs.parent_l;
+    s.range_lo = bs.range_lo;
+    s.range_hi = bs.range_hi;
+    s.ilo = bs.ilo;
+    s.ihi = bs.ihi;
+    s.cost = bs.cost;
+    s.collapse = bs.collapse;
+    s.arrive = bs.arrive;
+    s.cbounds = bs.cbounds;
+    s.cub_tmp = bs.sort_tmp;
+    s.cub_bytes = bvh_sort_temp_bytes(n);  // the sort of n items needs no more than the capacity's size
+    if (s.cub_bytes > bs.sort_tmp_bytes) return cudaErrorInvalidValue;
+    init_bounds_kernel<<<1, 32, 0, st>>>(s.cbounds);
+    tri_boxes_kernel<<<blocks(n), 256, 0, st>>>(vertices, indices, prims, items, n, s.lo, s.hi, bs.unsorted,
+                                                s.cbounds);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
+    if (e == cudaSuccess) {
+        gather_tris_kernel<<<blocks(n), 256, 0, st>>>(s.idx, n, bs.unsorted, tris, tri_base);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
 // World box of a transformed instance: the 8 transformed corners of its BLAS
 // root box, widened by a relative 1e-6 of the box size plus 1e-6 of the
 // largest coordinate so float rounding of the transform cannot make it

@@ -42,6 +42,33 @@ cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indi
                                const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
                                uint32_t tri_base, BvhResult* result_host, cudaStream_t st);
 
+// Scratch of one triangle-BVH build supplied by the caller instead of being
+// allocated (every pointer 256-byte aligned, sized for `capacity` items).
+struct BuildScratch {
+    uint32_t capacity;
+    float4 *lo, *hi, *ilo, *ihi;
+    uint32_t *morton_in, *morton, *idx_in, *idx, *range_lo, *range_hi, *collapse, *arrive, *cbounds;
+    int32_t *left, *right, *parent_i, *parent_l;
+    float* cost;
+    TriRec* unsorted;
+    void* sort_tmp;
+    size_t sort_tmp_bytes;
+};
+// Bytes of radix-sort temporary storage a build over n items needs.
+size_t bvh_sort_temp_bytes(uint32_t n);
+// Bytes a BuildScratch for `capacity` items takes when carved from one
+// 256-byte-aligned block (including the sort temporary storage).
+size_t bvh_scratch_bytes(uint32_t capacity);
+// Carves a BuildScratch for `capacity` items out of `base` (bvh_scratch_bytes
+// bytes, 256-byte aligned).
+BuildScratch bvh_scratch_carve(void* base, uint32_t capacity);
+// Same build as build_triangle_bvh, with n <= scratch.capacity and no device
+// allocation.
+cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_vertex* vertices,
+                                       const uint32_t* indices, const gbrt_priminfo* prims, const uint4* items,
+                                       uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
+                                       uint32_t tri_base, BvhResult* result_host, cudaStream_t st);
+
 // TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
 // the instance ids.
 cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_t* inst_ids, uint32_t n,

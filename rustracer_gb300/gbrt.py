@@ -56,7 +56,9 @@ SIGNATURES = {
     "gbrt_memcpy_d2h": (i32, [P, P, P, u64]),
     "gbrt_timer_begin": (i32, [P]),
     "gbrt_timer_end": (i32, [P, C.POINTER(C.c_double)]),
+    "gbrt_scene_rebuild_noalloc": (i32, [P, P]),
 }
+NOALLOC_MAX_TRIANGLES = 65536
 
 
 class GbrtError(RuntimeError):
@@ -199,6 +201,12 @@ class Scene:
     def skin_and_refit(self, skins):
         skins = np.ascontiguousarray(skins, T.SKIN)
         self.ctx.check(self.ctx.L.gbrt_skin_and_refit(self.h, _p(skins), len(skins)))
+
+    def rebuild_noalloc(self, d_vertices=None):
+        """Allocation-free rebuild of the world BVH (gbrt_scene_rebuild_noalloc);
+        d_vertices is a device pointer (int) to a full replacement vertex array,
+        or None to rebuild from the current vertices."""
+        self.ctx.check(self.ctx.L.gbrt_scene_rebuild_noalloc(self.h, None if d_vertices is None else P(d_vertices)))
 
     def update_lights(self, dlights, plights):
         d = np.ascontiguousarray(dlights, T.LIGHT)
