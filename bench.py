@@ -18,6 +18,7 @@ and the tone-mapped RGBA8 image copied back to host memory every step.
 shaders, all host threads) on a bounded sample of the same workload.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -34,6 +35,7 @@ sys.path.insert(0, ROOT)
 
 W, H, SPP, DEPTH, SUBDIV = 1920, 1080, 64, 8, 7
 WORKLOAD = f"icosphere{SUBDIV}_cornell_{W}x{H}_{SPP}spp_depth{DEPTH}"
+MODES = {"auto": 0, "megakernel": 1, "wavefront": 2}
 B_SHADE = 608  # algorithmic bytes per shaded hit (index, PrimInfo, 3 vertex subsets, material, new ray, path state)
 
 
@@ -174,7 +176,8 @@ def run_gpu(args):
         state["total"] += SPP
         ubo = np.asarray(sd.ubo(W, H, samples=SPP, total=state["total"], bounces=DEPTH, exposure=1.0)).reshape(())
         st = np.zeros((), gbrt.T.STATS)
-        ctx.check(ctx.L.gbrt_render(scene.h, gbrt._p(ubo), acc.h, out_ptr, gbrt._p(st)))
+        opts = gbrt.RenderOpts(MODES[args.mode], 0, None, None)
+        ctx.check(ctx.L.gbrt_render_ex(scene.h, gbrt._p(ubo), acc.h, out_ptr, gbrt._p(st), C.byref(opts)))
         return st
 
     def flush_l2():
@@ -199,6 +202,7 @@ def run_gpu(args):
             flush_l2()
             st = frame()
             rays += int(st["rays_total"])
+            launches = int(st["kernel_launches"])
             shaded += int(st["hits_shaded"])
             dev_ms += float(st["device_ms"])
         barrier()
@@ -235,7 +239,8 @@ def run_gpu(args):
     achieved = per_launch_bytes / (dev_ms / args.steps / 1e3) / 1e9
     traffic = traffic_from_profile()
     line = common_line(args, world, value, dev_ms / args.steps,
-                       {"kernel": "pt_megakernel", "wall_ms_per_step": wall / args.steps * 1e3})
+                       {"kernel": args.mode, "wall_ms_per_step": wall / args.steps * 1e3,
+                        "launches_per_step": launches})
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": traffic, "peak_source": peak_kind,
                         "bytes_per_ray": bray, "n_node": n_node, "n_tri": n_tri,
@@ -249,7 +254,7 @@ def run_gpu(args):
                                 "sample": f"{W}x{H} frame at {cs['spp']} spp ({cs['rays']} rays, "
                                           f"{cs['seconds']:.1f} s), same scene and depth"}
     line["clocks"] = clocks
-    line["gpu_launches"] = args.steps
+    line["gpu_launches"] = args.steps * launches
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -291,6 +296,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbrt", choices=["gbrt", "reference"])
+    ap.add_argument("--mode", default="auto", choices=list(MODES), help="kernel form (auto = wavefront)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
     ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -68,6 +69,8 @@ struct gbrt_ctx {
     std::string err;
     DevBuf counters;
     DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
+    DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums
+    WfState wf{};
     std::mutex mu;
 };
 
@@ -159,6 +162,43 @@ cudaError_t upload(DevBuf& b, const T* src, size_t n, cudaStream_t st) {
     cudaError_t e = b.alloc(n * sizeof(T));
     if (e != cudaSuccess || n == 0) return e;
     return cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+// Sizes the wavefront buffers for `cap` paths and `npix` pixels (grow only).
+cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t f4 = al((size_t)cap * sizeof(float4)), u1 = al((size_t)cap * 4);
+    const size_t bytes = 13 * f4 + 2 * u1 + al(kWfCounters * sizeof(uint32_t));
+    if (c->wf.cap < cap || c->wf_mem.bytes < bytes) {
+        cudaError_t e = c->wf_mem.alloc(bytes);
+        if (e != cudaSuccess) {
+            c->wf.cap = 0;
+            return e;
+        }
+        char* p = c->wf_mem.as<char>();
+        auto take = [&](size_t b) { void* r = p; p += b; return r; };
+        WfState& w = c->wf;
+        w.ray_o[0] = (float4*)take(f4);
+        w.ray_o[1] = (float4*)take(f4);
+        w.ray_d[0] = (float4*)take(f4);
+        w.ray_d[1] = (float4*)take(f4);
+        w.hit = (float4*)take(f4);
+        w.tp = (float4*)take(f4);
+        w.rad = (float4*)take(f4);
+        w.hp = (float4*)take(f4);
+        w.rng = (uint4*)take(f4);
+        w.sh_o = (float4*)take(f4);
+        w.sh_d = (float4*)take(f4);
+        w.sh_e = (float4*)take(f4);
+        w.sh_c = (float4*)take(f4);
+        w.hit_prim = (uint32_t*)take(u1);
+        w.sh_tp = (float*)take(u1);
+        w.counts = (uint32_t*)take(al(kWfCounters * sizeof(uint32_t)));
+        w.cap = cap;
+    }
+    cudaError_t e = c->wf_frame.reserve(npix * sizeof(float4));
+    c->wf.frame_sum = c->wf_frame.as<float4>();
+    return e;
 }
 
 void refresh_view(gbrt_scene* s) {
@@ -369,6 +409,7 @@ int gbrt_ctx_create(int device, gbrt_ctx** out) {
         lut[i] = (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
     }
     if ((e = init_render_constants(lut)) != cudaSuccess) return bail(e, "constants");
+    if ((e = init_wavefront_constants(lut)) != cudaSuccess) return bail(e, "constants");
     *out = c;
     return GBRT_OK;
 }
@@ -384,6 +425,8 @@ int gbrt_ctx_destroy(gbrt_ctx* c) {
         c->scratch_img.release();
         c->scratch_samples.release();
         c->scratch_phits.release();
+        c->wf_mem.release();
+        c->wf_frame.release();
         if (c->ev0) cudaEventDestroy(c->ev0);
         if (c->ev1) cudaEventDestroy(c->ev1);
         if (c->tb0) cudaEventDestroy(c->tb0);
@@ -646,7 +689,21 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     }
     CU(c, cudaMemsetAsync(out.counters, 0, sizeof(DeviceCounters), st), "memset");
     CU(c, cudaEventRecord(c->ev0, st), "event");
-    CU(c, launch_megakernel(s->view, *ubo, out, st), "megakernel launch");
+    const uint32_t mode = opts ? opts->mode : GBRT_MODE_AUTO;
+    const bool wave = (mode == GBRT_MODE_WAVEFRONT || mode == GBRT_MODE_AUTO) && ubo->number_of_bounces <= 31;
+    if (mode == GBRT_MODE_WAVEFRONT && !wave) return fail(c, GBRT_E_INVALID, "the wavefront form handles at most 31 bounces");
+    uint32_t launches = 1;
+    if (wave) {
+        const uint64_t paths = (uint64_t)npix * ns;
+        const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
+        CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
+        CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st), "wavefront launch");
+        const uint64_t npw = std::min<uint64_t>(npix, cap), k = cap / npw;
+        const uint64_t waves = ((npix + npw - 1) / npw) * ((ns + k - 1) / k);
+        launches = (uint32_t)(waves * (2 + 3 * ubo->number_of_bounces) + 1);
+    } else {
+        CU(c, launch_megakernel(s->view, *ubo, out, st), "megakernel launch");
+    }
     CU(c, cudaEventRecord(c->ev1, st), "event");
     if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
     if (out.sample_radiance)
@@ -662,7 +719,7 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     CU(c, cudaStreamSynchronize(st), "render");
     float ms = 0.0f;
     CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
-    fill_stats(stats, dc, ms, 1);
+    fill_stats(stats, dc, ms, launches);
     if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit (status " +
                                                             std::to_string(dc.status) + ")");
     return GBRT_OK;

@@ -20,6 +20,31 @@ struct RenderOut {
     DeviceCounters* counters;  // required
 };
 
+// wavefront.cu: device buffers of the wavefront path tracer, `cap` paths.
+constexpr int kWfCounters = 128;
+struct WfState {
+    uint32_t cap;
+    float4* ray_o[2];   // extension queues (ping-pong): origin
+    float4* ray_d[2];   //   direction, path id in .w
+    float4* hit;        // t, u, v, instance id
+    uint32_t* hit_prim;
+    float4* tp;         // per path: throughput, Ray.t
+    float4* rad;        //   radiance, volume_dis
+    float4* hp;         //   hit point, RandomSeed
+    uint4* rng;         //   pixel-stream counter, ray-stream counter, ray-stream z
+    float4* sh_o;       // shadow queue: origin, tmax
+    float4* sh_d;       //   direction, path id
+    float4* sh_e;       //   emission E, throughput.x
+    float4* sh_c;       //   NEE term C, throughput.y
+    float* sh_tp;       //   throughput.z
+    uint32_t* counts;   // kWfCounters queue lengths and fetch cursors
+    float4* frame_sum;  // per pixel: sum of the frame's samples, last Ray.t
+};
+size_t wavefront_bytes_per_path();
+cudaError_t init_wavefront_constants(const float* srgb_lut);
+cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
+                             cudaStream_t stream);
+
 // render.cu
 cudaError_t init_render_constants(const float* srgb_lut);
 cudaError_t launch_megakernel(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, cudaStream_t st);
