@@ -145,14 +145,17 @@ def common_line(args, n, value, ms_per_step, extra_cfg=None):
             "config": cfg}
 
 
-def traffic_from_profile():
-    """dram bytes per launch of pt_megakernel from the committed ncu summary
-    (profiles/pt_megakernel_icosphere.json), scaled to one full launch."""
-    p = os.path.join(ROOT, "profiles", "pt_megakernel_icosphere.json")
+def traffic_from_profile(kernel):
+    """DRAM bytes (read + write) per launch of `kernel` at this workload, from
+    the committed ncu summary profiles/dram_traffic_icosphere7.json (null when
+    that kernel has no capture)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_icosphere7.json")
     if not os.path.exists(p):
         return None
-    d = json.load(open(p))
-    return d.get("dram_bytes_per_full_launch")
+    d = json.load(open(p)).get(kernel)
+    if not d or (d.get("width"), d.get("height"), d.get("spp")) != (W, H, SPP):
+        return None
+    return d.get("dram_bytes_per_launch")
 
 
 def run_gpu(args):
@@ -172,11 +175,11 @@ def run_gpu(args):
     pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
     state = {"total": 0}
 
-    def frame(out_ptr=None):
+    def frame(out_ptr=None, timed=False):
         state["total"] += SPP
         ubo = np.asarray(sd.ubo(W, H, samples=SPP, total=state["total"], bounces=DEPTH, exposure=1.0)).reshape(())
         st = np.zeros((), gbrt.T.STATS)
-        opts = gbrt.RenderOpts(MODES[args.mode], 0, None, None)
+        opts = gbrt.RenderOpts(MODES[args.mode], 1 if timed else 0, None, None)  # 1 = per-stage CUDA events
         ctx.check(ctx.L.gbrt_render_ex(scene.h, gbrt._p(ubo), acc.h, out_ptr, gbrt._p(st), C.byref(opts)))
         return st
 
@@ -196,15 +199,22 @@ def run_gpu(args):
     barrier()
     rays = shaded = 0
     dev_ms = 0.0
+    stage_ms, stage_rays, visits = [0.0] * 4, [0, 0, 0], [0, 0]
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             flush_l2()
-            st = frame()
+            st = frame(timed=True)
             rays += int(st["rays_total"])
             launches = int(st["kernel_launches"])
             shaded += int(st["hits_shaded"])
             dev_ms += float(st["device_ms"])
+            for k in range(4):
+                stage_ms[k] += float(st["stage_ms"][k])
+            stage_rays[0] += int(st["rays_camera"] + st["rays_extension"])
+            stage_rays[2] += int(st["rays_shadow"])
+            visits[0] += int(st["node_visits"])
+            visits[1] += int(st["tri_tests"])
         barrier()
         wall = time.perf_counter() - t0
     clocks = clk.summary()
@@ -235,17 +245,33 @@ def run_gpu(args):
     bray, n_node, n_tri = b_ray(cs)
     value = tot_rays / (dev_ms / 1e3) / 1e6
     peak, peak_kind = measured_peaks()
-    per_launch_bytes = (rays * bray + shaded * B_SHADE) / args.steps
-    achieved = per_launch_bytes / (dev_ms / args.steps / 1e3) / 1e9
-    traffic = traffic_from_profile()
+    if sum(stage_ms) > 0:  # wavefront: the dominant stage kernel, bytes from its own units
+        names = ["wf_extend", "wf_shade", "wf_shadow"]
+        stage_bytes = [stage_rays[0] * bray, shaded * B_SHADE, stage_rays[2] * bray]
+        stages = {names[k]: {"ms_per_step": stage_ms[k] / args.steps,
+                             "achieved_gbs": stage_bytes[k] / (stage_ms[k] / 1e3) / 1e9 if stage_ms[k] else None,
+                             "share": stage_ms[k] / sum(stage_ms)} for k in range(3)}
+        stages["other"] = {"ms_per_step": stage_ms[3] / args.steps, "share": stage_ms[3] / sum(stage_ms)}
+        dom = max(range(3), key=lambda k: stage_ms[k])
+        kernel_name = names[dom]
+        achieved = stage_bytes[dom] / (stage_ms[dom] / 1e3) / 1e9
+    else:
+        stages = None
+        kernel_name = "pt_megakernel"
+        achieved = (rays * bray + shaded * B_SHADE) / (dev_ms / 1e3) / 1e9
+    traffic = traffic_from_profile(kernel_name)
     line = common_line(args, world, value, dev_ms / args.steps,
                        {"kernel": args.mode, "wall_ms_per_step": wall / args.steps * 1e3,
                         "launches_per_step": launches})
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": traffic, "peak_source": peak_kind,
                         "bytes_per_ray": bray, "n_node": n_node, "n_tri": n_tri,
-                        "bytes_per_shaded_hit": B_SHADE, "kernel": "pt_megakernel",
-                        "hbm_roofline_mrays": peak * 1e3 / bray}
+                        "bytes_per_shaded_hit": B_SHADE, "kernel": kernel_name,
+                        "hbm_roofline_mrays": peak * 1e3 / bray,
+                        "gpu_node_visits_per_ray": visits[0] / max(rays, 1),
+                        "gpu_tri_tests_per_ray": visits[1] / max(rays, 1)}
+    if stages:
+        line["roofline"]["stages"] = stages
     line["e2e"] = {"value": tot_e2e / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(gbrt.T.UBO.itemsize),
                    "d2h_bytes_per_step": W * H * 4}
     if world == 1:

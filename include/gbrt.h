@@ -242,6 +242,10 @@ typedef struct gbrt_stats {
     double   device_ms;       /* CUDA-event time of the device work */
     uint32_t kernel_launches;
     uint32_t device_status;   /* 0, or GBRT_STATUS_* bits reported by kernels */
+    uint64_t node_visits;     /* BVH inner nodes visited by all traversals */
+    uint64_t tri_tests;       /* ray-triangle tests */
+    double   stage_ms[4];     /* with GBRT_RENDER_STAGE_TIMING (wavefront form):
+                                 extend, shade, shadow, other kernels */
 } gbrt_stats;
 
 #define GBRT_STATUS_STACK_OVERFLOW 0x1u
@@ -252,9 +256,10 @@ typedef struct gbrt_stats {
 #define GBRT_MODE_AUTO       0
 #define GBRT_MODE_MEGAKERNEL 1
 #define GBRT_MODE_WAVEFRONT  2
+#define GBRT_RENDER_STAGE_TIMING 0x1u  /* gbrt_render_opts.flags: CUDA-event time per stage */
 typedef struct gbrt_render_opts {
     uint32_t mode;            /* GBRT_MODE_* */
-    uint32_t flags;           /* reserved, 0 */
+    uint32_t flags;           /* GBRT_RENDER_STAGE_TIMING or 0 */
     /* Optional debug outputs (host memory, may be NULL):
      * sample_radiance: width*height*number_of_samples*3 floats, per-sample
      *                  path radiance, laid out [pixel][sample][rgb];

@@ -28,6 +28,7 @@ static_assert(sizeof(gbrt_ubo) == 324, "UniformBufferObject is 324 B");
 static_assert(sizeof(gbrt_instance) == 64, "VkAccelerationStructureInstanceKHR is 64 B");
 static_assert(sizeof(gbrt_skin_raw) == 16384, "Skin is 256 mat4");
 static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records");
+static_assert(sizeof(gbrt_stats) == 104, "stats record");
 
 namespace {
 
@@ -68,9 +69,11 @@ struct gbrt_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, tb0 = nullptr, tb1 = nullptr;
     std::string err;
     DevBuf counters;
+    DevBuf trace_work;  // fetch cursor of the persistent ray-query kernel
     DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
     DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums
     WfState wf{};
+    StageTimer timer;
     std::mutex mu;
 };
 
@@ -89,6 +92,8 @@ struct gbrt_scene {
     bool all_opaque = true;
     // acceleration structures
     DevBuf nodes, tris, inst, items;
+    DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
+    uint32_t cw_count = 0;
     bool built = false;
     DevScene view{};
     ~gbrt_scene() {
@@ -219,6 +224,8 @@ void refresh_view(gbrt_scene* s) {
     v.np = s->np;
     v.sky = s->sky.as<uchar4>();
     v.sky_size = s->sky_size;
+    v.cw_nodes = s->cw_count ? s->cw_nodes.as<CwNode>() : nullptr;
+    v.cw_tris = s->cw_count ? s->cw_tris.as<TriRec>() : nullptr;
 }
 
 // Builds the merged world BVH, the BLASes of transformed instances and the
@@ -299,6 +306,17 @@ int build_all(gbrt_scene* s) {
         v.world_root = r.root;
         v.world_lo = r.lo;
         v.world_hi = r.hi;
+        const size_t nw = world_items.size();
+        CU(c, s->cw_nodes.alloc(nw * sizeof(CwNode)), "cudaMalloc(wide nodes)");
+        CU(c, s->cw_tris.alloc(nw * sizeof(TriRec)), "cudaMalloc(wide triangles)");
+        CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                   s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)nw,
+                                   s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), &s->cw_count, st),
+           "build wide world BVH");
+    } else {
+        s->cw_nodes.release();
+        s->cw_tris.release();
+        s->cw_count = 0;
     }
     // BLASes + TLAS
     if (!tlas_ids.empty()) {
@@ -368,6 +386,9 @@ void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t la
     st->device_ms = ms;
     st->kernel_launches = launches;
     st->device_status = dc.status;
+    st->node_visits = dc.nodes;
+    st->tri_tests = dc.tris;
+    for (int k = 0; k < 4; ++k) st->stage_ms[k] = 0.0;
 }
 
 }  // namespace
@@ -403,6 +424,7 @@ int gbrt_ctx_create(int device, gbrt_ctx** out) {
     if ((e = cudaEventCreate(&c->tb0)) != cudaSuccess) return bail(e, "event");
     if ((e = cudaEventCreate(&c->tb1)) != cudaSuccess) return bail(e, "event");
     if ((e = c->counters.alloc(sizeof(DeviceCounters))) != cudaSuccess) return bail(e, "counters");
+    if ((e = c->trace_work.alloc(256)) != cudaSuccess) return bail(e, "counters");
     float lut[256];
     for (int i = 0; i < 256; ++i) {
         double v = i / 255.0;
@@ -420,6 +442,7 @@ int gbrt_ctx_destroy(gbrt_ctx* c) {
         DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
         c->counters.release();
+        c->trace_work.release();
         c->scratch_rays.release();
         c->scratch_hits.release();
         c->scratch_img.release();
@@ -427,6 +450,7 @@ int gbrt_ctx_destroy(gbrt_ctx* c) {
         c->scratch_phits.release();
         c->wf_mem.release();
         c->wf_frame.release();
+        stage_timer_free(c->timer);
         if (c->ev0) cudaEventDestroy(c->ev0);
         if (c->ev1) cudaEventDestroy(c->ev1);
         if (c->tb0) cudaEventDestroy(c->tb0);
@@ -697,7 +721,8 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
         const uint64_t paths = (uint64_t)npix * ns;
         const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
         CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
-        CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st), "wavefront launch");
+        const bool timed = opts && (opts->flags & GBRT_RENDER_STAGE_TIMING);
+        CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, timed ? &c->timer : nullptr), "wavefront launch");
         const uint64_t npw = std::min<uint64_t>(npix, cap), k = cap / npw;
         const uint64_t waves = ((npix + npw - 1) / npw) * ((ns + k - 1) / k);
         launches = (uint32_t)(waves * (2 + 3 * ubo->number_of_bounces) + 1);
@@ -720,6 +745,8 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     float ms = 0.0f;
     CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
     fill_stats(stats, dc, ms, launches);
+    if (stats && wave && opts && (opts->flags & GBRT_RENDER_STAGE_TIMING))
+        CU(c, stage_timer_collect(c->timer, stats->stage_ms), "stage timing");
     if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit (status " +
                                                             std::to_string(dc.status) + ")");
     return GBRT_OK;
@@ -735,7 +762,9 @@ int gbrt_trace_rays_device(gbrt_scene* s, const gbrt_ray* d_rays, uint32_t n, ui
     if (n && (!d_rays || !d_hits)) return fail(c, GBRT_E_INVALID, "rays or hits is NULL");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tracing");
     DeviceGuard g(c->device);
-    CU(c, launch_trace_rays(s->view, d_rays, n, flags, d_hits, nullptr, c->stream), "trace launch");
+    CU(c, launch_trace_rays_persistent(s->view, d_rays, n, flags, d_hits, c->trace_work.as<uint32_t>(), nullptr,
+                                       c->stream),
+       "trace launch");
     return GBRT_OK;
 }
 
@@ -753,8 +782,8 @@ int gbrt_trace_rays(gbrt_scene* s, const gbrt_ray* rays, uint32_t n, uint32_t fl
     CU(c, cudaMemsetAsync(dcnt, 0, sizeof(DeviceCounters), st), "memset");
     if (n) CU(c, cudaMemcpyAsync(c->scratch_rays.p, rays, n * sizeof(gbrt_ray), cudaMemcpyHostToDevice, st), "upload rays");
     CU(c, cudaEventRecord(c->ev0, st), "event");
-    CU(c, launch_trace_rays(s->view, c->scratch_rays.as<gbrt_ray>(), n, flags, c->scratch_hits.as<gbrt_hit>(), dcnt,
-                            st),
+    CU(c, launch_trace_rays_persistent(s->view, c->scratch_rays.as<gbrt_ray>(), n, flags,
+                                       c->scratch_hits.as<gbrt_hit>(), c->trace_work.as<uint32_t>(), dcnt, st),
        "trace launch");
     CU(c, cudaEventRecord(c->ev1, st), "event");
     if (n) CU(c, cudaMemcpyAsync(hits, c->scratch_hits.p, n * sizeof(gbrt_hit), cudaMemcpyDeviceToHost, st), "download hits");
@@ -886,5 +915,10 @@ extern "C" int gbrt_scene_rebuild_noalloc(gbrt_scene* s, const gbrt_vertex* d_ve
     s->view.world_root = r.root;
     s->view.world_lo = r.lo;
     s->view.world_hi = r.hi;
+    // the 8-wide copy of the world BVH now describes the old vertices: drop it
+    // so every traversal uses the rebuilt binary BVH
+    s->cw_count = 0;
+    s->view.cw_nodes = nullptr;
+    s->view.cw_tris = nullptr;
     return GBRT_OK;
 }

@@ -193,7 +193,7 @@ __device__ __forceinline__ float half_area(float3 l, float3 h) {
 __global__ void bottom_up_kernel(int n, const uint32_t* idx, const float4* lo, const float4* hi,
                                  const int32_t* left, const int32_t* right, const int32_t* parent_i,
                                  const int32_t* parent_l, const uint32_t* rlo, const uint32_t* rhi, float4* ilo,
-                                 float4* ihi, float* cost, uint32_t* collapse, uint32_t* arrive) {
+                                 float4* ihi, float* cost, uint32_t* collapse, uint32_t* arrive, uint32_t max_leaf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int p = parent_l[i];
@@ -222,7 +222,7 @@ __global__ void bottom_up_kernel(int n, const uint32_t* idx, const float4* lo, c
         const uint32_t count = rhi[p] - rlo[p] + 1u;
         const float split = kCostTraverse * a + c[0] + c[1];
         const float as_leaf = kCostTri * a * (float)count;
-        const bool col = count <= kMaxLeaf && as_leaf <= split;
+        const bool col = count <= max_leaf && as_leaf <= split;
         ilo[p] = f4(l, 0.0f);
         ihi[p] = f4(h, 0.0f);
         cost[p] = col ? as_leaf : split;
@@ -332,10 +332,10 @@ void scratch_free(Scratch& s, cudaStream_t st) {
         if (p) cudaFreeAsync(p, st);
 }
 
-// Common tail: sort, radix tree, bottom-up, emit.  Item boxes in s.lo/hi and
+// Morton codes, sort, radix tree and the bottom-up pass (boxes, SAH costs,
+// leaf collapse with at most max_leaf items).  Item boxes in s.lo/hi and
 // centroid bounds in s.cbounds must be ready.
-cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_base, uint32_t tri_base,
-                         BvhResult* res, cudaStream_t st) {
+cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t st) {
     morton_kernel<<<blocks(n), 256, 0, st>>>(s.lo, s.hi, n, s.cbounds, s.morton_in, s.idx_in);
     CK(cudaGetLastError());
     CK(cub::DeviceRadixSort::SortPairs(s.cub_tmp, s.cub_bytes, s.morton_in, s.morton, s.idx_in, s.idx, (int)n, 0,
@@ -347,8 +347,17 @@ cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_ba
         CK(cudaMemsetAsync(s.arrive, 0, (n - 1) * sizeof(uint32_t), st));
         bottom_up_kernel<<<blocks(n), 256, 0, st>>>((int)n, s.idx, s.lo, s.hi, s.left, s.right, s.parent_i,
                                                    s.parent_l, s.range_lo, s.range_hi, s.ilo, s.ihi, s.cost,
-                                                   s.collapse, s.arrive);
+                                                   s.collapse, s.arrive, max_leaf);
         CK(cudaGetLastError());
+    }
+    return cudaSuccess;
+}
+
+// Common tail: radix tree with leaves of up to kMaxLeaf items, emit BNode2.
+cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_base, uint32_t tri_base,
+                         BvhResult* res, cudaStream_t st) {
+    CK(radix_tree(s, n, kMaxLeaf, st));
+    if (n > 1) {
         emit_nodes_kernel<<<blocks(n - 1), 256, 0, st>>>((int)n, s.idx, s.lo, s.hi, s.left, s.right, s.range_lo,
                                                         s.range_hi, s.ilo, s.ihi, s.collapse, nodes, node_base,
                                                         tri_base);
@@ -548,4 +557,8 @@ cudaError_t instance_world_boxes(const DevInstance* inst, const uint32_t* ids, c
     return cudaGetLastError();
 }
 
+}  // namespace gbrt
+
+namespace gbrt {
+#include "cwbvh_build.inc"
 }  // namespace gbrt

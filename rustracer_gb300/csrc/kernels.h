@@ -40,10 +40,25 @@ struct WfState {
     uint32_t* counts;   // kWfCounters queue lengths and fetch cursors
     float4* frame_sum;  // per pixel: sum of the frame's samples, last Ray.t
 };
+// CUDA-event pairs around every wavefront launch, grouped by stage
+// (0 extend, 1 shade, 2 shadow, 3 other).  Events are created on demand and
+// reused across frames.
+struct StageTimer {
+    cudaEvent_t* ev = nullptr;  // 2 * capacity events
+    int* stage = nullptr;       // stage of each pair
+    int capacity = 0, used = 0;
+};
 size_t wavefront_bytes_per_path();
 cudaError_t init_wavefront_constants(const float* srgb_lut);
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
-                             cudaStream_t stream);
+                             cudaStream_t stream, StageTimer* timer = nullptr);
+// Ray queries through the persistent world traversal (8-wide when built);
+// `work` is one device word used as the fetch cursor.
+cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays, uint32_t n, uint32_t flags,
+                                         gbrt_hit* hits, uint32_t* work, DeviceCounters* cnt, cudaStream_t st);
+// Sums the recorded pairs per stage (call after the stream synchronised).
+cudaError_t stage_timer_collect(StageTimer& t, double ms[4]);
+void stage_timer_free(StageTimer& t);
 
 // render.cu
 cudaError_t init_render_constants(const float* srgb_lut);
@@ -93,6 +108,13 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_v
                                        const uint32_t* indices, const gbrt_priminfo* prims, const uint4* items,
                                        uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
                                        uint32_t tri_base, BvhResult* result_host, cudaStream_t st);
+
+// Compressed 8-wide BVH over n triangle items: nodes (capacity n, root at 0)
+// and their triangles (n slots, node-leaf order); *nodes_used (host) gets
+// the node count.
+cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
+                                 const uint4* items, uint32_t n, CwNode* nodes, TriRec* tris, uint32_t* nodes_used,
+                                 cudaStream_t st);
 
 // TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
 // the instance ids.

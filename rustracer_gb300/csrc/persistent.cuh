@@ -1,0 +1,359 @@
+// persistent.cuh — persistent-lane traversal of the world BVH with ray
+// refill (after Aila & Laine 2009, "Understanding the Efficiency of Ray
+// Traversal on GPUs").
+//
+// Every lane owns one ray at a time.  Each outer iteration a lane descends
+// inner nodes until it reaches a leaf (or its stack empties), then tests that
+// leaf's triangles (while-while).  A lane whose ray finished goes idle; once
+// at least kRefill lanes of the warp are idle they take new rays from the
+// queue together (one atomic per warp).  The warp therefore no longer waits
+// for its longest ray, which is what kept SIMT efficiency low when a warp
+// traced a fixed group of 32 rays.  The stack holds (node, entry distance)
+// pairs so entries behind the current closest hit are dropped when popped.
+//
+// Scenes with transformed instances finish each ray with the two-level pass
+// of trace.cuh after the world BVH (same exactness rules).
+#pragma once
+#include "trace.cuh"
+
+namespace gbrt {
+
+constexpr int kEmpty = 0x7FFFFFFF;  // "stack exhausted"
+constexpr uint32_t kRefill = 8;     // idle lanes that trigger a refill
+
+// Loader: bool load(uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx)
+// Finisher: void finish(uint32_t q, bool hit, const Hit& h)
+template <bool kAny, class Loader, class Finisher>
+GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts,
+                           Loader&& load, Finisher&& finish) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+    int stack_node[kStack];
+    float stack_t[kStack];
+    bool has = false, exhausted = false;
+    uint32_t q = 0;
+    TRay r;
+    Hit best;
+    AnyCtx ctx{0, 0, 0, 0};
+    float tmin = 0.0f, tmax = 0.0f;
+    int cur = kEmpty, sp = 0;
+    uint32_t iter = 0;
+    for (;;) {
+        if (!exhausted) {
+            const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !has);
+            if (__popc(idle) >= (int)kRefill) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(work, (uint32_t)__popc(idle));
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base + __popc(idle) >= n) exhausted = true;
+                if (!has) {
+                    q = base + __popc(idle & ((1u << lane) - 1u));
+                    if (q < n) {
+                        float3 o, d;
+                        load(q, o, d, tmin, tmax, ctx);
+                        best.t = tmax;
+                        best.u = best.v = 0.0f;
+                        best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
+                        iter = 0;
+                        if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
+                            finish(q, false, best);
+                        } else {
+                            has = true;
+                            setup_ray(r, o, d);
+                            sp = 0;
+                            cur = kEmpty;
+                            float tn;
+                            if (s.has_world && box_hit(r, s.world_lo.x, s.world_hi.x, s.world_lo.y, s.world_hi.y,
+                                                       s.world_lo.z, s.world_hi.z, tmin, best.t, tn))
+                                cur = s.world_root;
+                        }
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, has)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!has) continue;
+        // --- descend to a leaf ------------------------------------------------
+        int leaf = 0;
+        while (cur != kEmpty) {
+            if (++iter > kMaxIter) {
+                ts.status |= GBRT_STATUS_ITER_LIMIT;
+                cur = kEmpty;
+                break;
+            }
+            if (cur < 0) {  // leaf: take it, resume from the stack afterwards
+                leaf = cur;
+                cur = kEmpty;
+                while (sp > 0) {
+                    --sp;
+                    if (stack_t[sp] <= best.t) {
+                        cur = stack_node[sp];
+                        break;
+                    }
+                }
+                break;
+            }
+            const BNode2* nd = s.nodes + cur;
+            const float4 a = __ldg(&nd->lxy), b = __ldg(&nd->rxy), z = __ldg(&nd->lrz);
+            const int4 c = __ldg(&nd->c);
+            ts.nodes++;
+            float tn0, tn1;
+            const bool h0 = box_hit(r, a.x, a.y, a.z, a.w, z.x, z.y, tmin, best.t, tn0);
+            const bool h1 = box_hit(r, b.x, b.y, b.z, b.w, z.z, z.w, tmin, best.t, tn1);
+            if (h0 && h1) {
+                const bool swap = tn1 < tn0;
+                if (sp < kStack) {
+                    stack_node[sp] = swap ? c.x : c.y;
+                    stack_t[sp] = swap ? tn0 : tn1;
+                    ++sp;
+                } else {
+                    ts.status |= GBRT_STATUS_STACK_OVERFLOW;
+                }
+                cur = swap ? c.y : c.x;
+            } else if (h0) {
+                cur = c.x;
+            } else if (h1) {
+                cur = c.y;
+            } else {
+                cur = kEmpty;
+                while (sp > 0) {
+                    --sp;
+                    if (stack_t[sp] <= best.t) {
+                        cur = stack_node[sp];
+                        break;
+                    }
+                }
+            }
+        }
+        // --- test the leaf ------------------------------------------------------
+        bool done = false;
+        if (leaf != 0) {
+            const uint32_t first = leaf_first(leaf), count = leaf_count(leaf);
+            for (uint32_t i = 0; i < count; ++i) {
+                const TriRec* tr = s.tris + first + i;
+                const float4 pa = __ldg(&tr->a), pb = __ldg(&tr->b), pc = __ldg(&tr->c);
+                ts.tris++;
+                float t, u, v;
+                if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                const uint32_t inst = __float_as_uint(pa.w);
+                const uint32_t prim = __float_as_uint(pb.w);
+                const uint32_t gw = __float_as_uint(pc.w);
+                if (!closer(t, inst, prim, best)) continue;
+                if (test_alpha && !(gw >> 31) && anyhit_ignore(s, s.inst[inst].custom, prim, inst, u, v, ctx)) continue;
+                best.t = t;
+                best.u = u;
+                best.v = v;
+                best.inst = inst;
+                best.prim = prim;
+                best.bgeo = gw & 0x7FFFFFFFu;
+                if (kAny) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (!done && cur == kEmpty) done = true;
+        if (done) {
+            if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu)) {
+                // transformed instances: finish the ray with the two-level pass
+                trace_tlas<kAny>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);
+            }
+            finish(q, best.inst != 0xFFFFFFFFu, best);
+            has = false;
+        }
+    }
+}
+
+}  // namespace gbrt
+
+namespace gbrt {
+
+constexpr int kCwStack = 32;
+
+// Byte k of an 8-byte group (lo word = bytes 0..3) as the float
+// 1 + q * 2^-15, in one byte permute: result bytes (from low) = 0x00, q, 0x80,
+// 0x3F, i.e. 0x3F80qq00.
+GB_D float cw_q(uint32_t lo, uint32_t hi, int k) {
+    const uint32_t w = k < 4 ? lo : hi;
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)(k & 3) << 4)));
+}
+
+// Intersects the 8 children of wide node `node`: returns the hit mask (bits
+// 24 + (slot ^ oct) for inner children, triangle bits 0..23 for leaves) and
+// the node's child base, triangle base and inner-slot mask.
+GB_D uint32_t cw_intersect(const DevScene& s, uint32_t node, const TRay& r, uint32_t oct, float tmin, float tmax,
+                           uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
+    const uint4* np = reinterpret_cast<const uint4*>(s.cw_nodes + node);
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    child_base = w1.x;
+    tri_base = w1.y;
+    imask = w0.w >> 24;
+    // per axis: t = o + q * s = fma(1 + q 2^-15, 2^15 s, o - 2^15 s).  An axis the
+    // ray is parallel to (d = 0) gives (-inf, +inf) and the origin must lie
+    // inside that child's slab instead.
+    const float scx = __uint_as_float((w0.w & 0xFFu) << 23);
+    const float scy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23);
+    const float scz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23);
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const bool zx = r.d.x == 0.0f, zy = r.d.y == 0.0f, zz = r.d.z == 0.0f;
+    const float Sx = zx ? 0.0f : 32768.0f * (scx * r.inv.x);
+    const float Sy = zy ? 0.0f : 32768.0f * (scy * r.inv.y);
+    const float Sz = zz ? 0.0f : 32768.0f * (scz * r.inv.z);
+    const float Ox = (px - r.o.x) * r.inv.x - Sx, Oy = (py - r.o.y) * r.inv.y - Sy, Oz = (pz - r.o.z) * r.inv.z - Sz;
+    const float Oxn = zx ? -INFINITY : Ox, Oxf = zx ? INFINITY : Ox;
+    const float Oyn = zy ? -INFINITY : Oy, Oyf = zy ? INFINITY : Oy;
+    const float Ozn = zz ? -INFINITY : Oz, Ozf = zz ? INFINITY : Oz;
+    const bool parallel = zx || zy || zz;
+    // near / far planes per axis by direction sign
+    const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
+    const uint32_t lnx0 = nx ? w3.z : w2.x, lnx1 = nx ? w3.w : w2.y, lfx0 = nx ? w2.x : w3.z, lfx1 = nx ? w2.y : w3.w;
+    const uint32_t lny0 = ny ? w4.x : w2.z, lny1 = ny ? w4.y : w2.w, lfy0 = ny ? w2.z : w4.x, lfy1 = ny ? w2.w : w4.y;
+    const uint32_t lnz0 = nz ? w4.z : w3.x, lnz1 = nz ? w4.w : w3.y, lfz0 = nz ? w3.x : w4.z, lfz1 = nz ? w3.y : w4.w;
+    uint32_t hits = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t meta = ((k < 4 ? w1.z : w1.w) >> (8 * (k & 3))) & 0xFFu;
+        const float tnx = fmaf(cw_q(lnx0, lnx1, k), Sx, Oxn), tfx = fmaf(cw_q(lfx0, lfx1, k), Sx, Oxf);
+        const float tny = fmaf(cw_q(lny0, lny1, k), Sy, Oyn), tfy = fmaf(cw_q(lfy0, lfy1, k), Sy, Oyf);
+        const float tnz = fmaf(cw_q(lnz0, lnz1, k), Sz, Ozn), tfz = fmaf(cw_q(lfz0, lfz1, k), Sz, Ozf);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        bool inside = true;
+        if (parallel) {  // decoded slab of each parallel axis must contain the origin
+            auto in = [&](bool z, uint32_t lo0, uint32_t lo1, uint32_t hi0, uint32_t hi1, float p, float sc, float o) {
+                if (!z) return true;
+                const float ql = (cw_q(lo0, lo1, k) - 1.0f) * 32768.0f, qh = (cw_q(hi0, hi1, k) - 1.0f) * 32768.0f;
+                return o >= p + ql * sc && o <= p + qh * sc;
+            };
+            inside = in(zx, w2.x, w2.y, w3.z, w3.w, px, scx, r.o.x) && in(zy, w2.z, w2.w, w4.x, w4.y, py, scy, r.o.y) &&
+                     in(zz, w3.x, w3.y, w4.z, w4.w, pz, scz, r.o.z);
+        }
+        // empty slots (meta 0) contribute no bit
+        const uint32_t low = meta & 0x1Fu;
+        const uint32_t bits = low >= 24u ? (1u << (24u + ((uint32_t)k ^ oct))) : ((meta >> 5) << low);
+        hits |= (tn <= tf && inside) ? bits : 0u;
+    }
+    return hits;
+}
+
+// Persistent-lane traversal of the 8-wide world BVH; same interface and
+// refill policy as persistent_trace.
+template <bool kAny, class Loader, class Finisher>
+GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts,
+                              Loader&& load, Finisher&& finish) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+    uint2 stack[kCwStack];
+    bool has = false, exhausted = false;
+    uint32_t q = 0, oct = 0;
+    TRay r;
+    Hit best;
+    AnyCtx ctx{0, 0, 0, 0};
+    float tmin = 0.0f, tmax = 0.0f;
+    uint2 ng = make_uint2(0, 0);
+    int sp = 0;
+    uint32_t iter = 0;
+    for (;;) {
+        if (!exhausted) {
+            const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !has);
+            if (__popc(idle) >= (int)kRefill) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(work, (uint32_t)__popc(idle));
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base + __popc(idle) >= n) exhausted = true;
+                if (!has) {
+                    q = base + __popc(idle & ((1u << lane) - 1u));
+                    if (q < n) {
+                        float3 o, d;
+                        load(q, o, d, tmin, tmax, ctx);
+                        best.t = tmax;
+                        best.u = best.v = 0.0f;
+                        best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
+                        iter = 0;
+                        if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
+                            finish(q, false, best);
+                        } else {
+                            has = true;
+                            setup_ray(r, o, d);
+                            oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+                            sp = 0;
+                            // virtual parent: one inner child (the root, node 0) in slot 0
+                            ng = s.has_world ? make_uint2(0u, (1u << (24u + oct)) | 1u) : make_uint2(0u, 0u);
+                        }
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xFFFFFFFFu, has)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!has) continue;
+        bool done = false;
+        while (!(ng.y & 0xFF000000u) && sp > 0) ng = stack[--sp];
+        if (!(ng.y & 0xFF000000u)) {
+            done = true;
+        } else if (++iter > kMaxIter) {
+            ts.status |= GBRT_STATUS_ITER_LIMIT;
+            done = true;
+        } else {
+            const uint32_t bit = __ffs(ng.y & 0xFF000000u) - 1u;
+            ng.y &= ~(1u << bit);
+            const uint32_t slot = (bit - 24u) ^ oct;
+            const uint32_t child = ng.x + __popc((ng.y & 0xFFu) & ((1u << slot) - 1u));
+            if (ng.y & 0xFF000000u) {
+                if (sp < kCwStack) stack[sp++] = ng;
+                else ts.status |= GBRT_STATUS_STACK_OVERFLOW;
+            }
+            uint32_t cb, tb, im;
+            const uint32_t hm = cw_intersect(s, child, r, oct, tmin, best.t, cb, tb, im);
+            ts.nodes++;
+            ng = make_uint2(cb, (hm & 0xFF000000u) | im);
+            uint32_t tri_bits = hm & 0x00FFFFFFu;
+            while (tri_bits) {
+                const uint32_t tbit = __ffs(tri_bits) - 1u;
+                tri_bits &= tri_bits - 1u;
+                const TriRec* tr = s.cw_tris + tb + tbit;
+                const float4 pa = __ldg(&tr->a), pb = __ldg(&tr->b), pc = __ldg(&tr->c);
+                ts.tris++;
+                float t, u, v;
+                if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                const uint32_t inst = __float_as_uint(pa.w);
+                const uint32_t prim = __float_as_uint(pb.w);
+                const uint32_t gw = __float_as_uint(pc.w);
+                if (!closer(t, inst, prim, best)) continue;
+                if (test_alpha && !(gw >> 31) && anyhit_ignore(s, s.inst[inst].custom, prim, inst, u, v, ctx))
+                    continue;
+                best.t = t;
+                best.u = u;
+                best.v = v;
+                best.inst = inst;
+                best.prim = prim;
+                best.bgeo = gw & 0x7FFFFFFFu;
+                if (kAny) {
+                    done = true;
+                    break;
+                }
+            }
+        }
+        if (done) {
+            if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu))
+                trace_tlas<kAny>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);
+            finish(q, best.inst != 0xFFFFFFFFu, best);
+            has = false;
+        }
+    }
+}
+
+// World traversal in the layout the scene carries (8-wide when built).
+template <bool kAny, bool kWide, class Loader, class Finisher>
+GB_D void world_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts, Loader&& load,
+                      Finisher&& finish) {
+    if (kWide) persistent_trace_cw<kAny>(s, n, work, flags, ts, load, finish);
+    else persistent_trace<kAny>(s, n, work, flags, ts, load, finish);
+}
+
+}  // namespace gbrt

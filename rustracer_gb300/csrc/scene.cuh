@@ -38,6 +38,27 @@ struct alignas(16) TriRec {
     float4 a, b, c;
 };
 
+// Compressed 8-wide BVH node (after Ylitie, Karras, Laine 2017, "Efficient
+// Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs"), 80 B,
+// fetched as five 16-byte loads.  Child boxes are 8-bit offsets on a
+// per-node grid: lo = p + qlo * 2^(e-127) per axis, rounded outward and
+// padded by one grid step at build time.  meta[s]: 0 = empty slot; inner
+// child = 0x20 | (24 + s); leaf = (unary triangle count << 5) | offset of its
+// first triangle from tri_base (count <= 3, offsets < 24).  Inner children
+// are stored contiguously from child_base in slot order; a ray of octant o
+// visits the inner children in increasing order of (slot ^ o).
+struct alignas(16) CwNode {
+    float p[3];
+    uint8_t e[3];
+    uint8_t imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(CwNode) == 80, "CwNode is 80 B");
+
 struct DevInstance {
     float xf[12];      // object-to-world, row-major 3x4
     float inv[12];     // world-to-object
@@ -62,6 +83,8 @@ struct DevScene {
     uint32_t ninst;
     int32_t world_root;   // node index or leaf code, valid when has_world
     int32_t tlas_root;    // valid when has_tlas
+    const CwNode* cw_nodes;  // 8-wide world BVH (root = node 0), null if not built
+    const TriRec* cw_tris;   //   its triangles, in node-leaf order
     uint32_t has_world;   // some identity instance exists
     uint32_t has_tlas;    // some transformed instance exists
     float4 world_lo, world_hi;  // bounds of the world BVH root

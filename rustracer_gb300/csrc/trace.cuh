@@ -212,28 +212,14 @@ GB_D bool traverse_bvh(const DevScene& s, int root, const TRay& r, float tmin, H
     }
 }
 
-// Full query: the merged world BVH, then the TLAS over transformed instances
-// (each BLAS traversed in object space with the world-to-object transform
-// applied unfused, like the oracle).
+// The TLAS part of a query: transformed instances, each BLAS traversed in
+// object space with the world-to-object transform applied unfused (like the
+// oracle), updating `best`.  Returns true when a terminate-on-first query
+// found a hit.
 template <bool kTerminateOnFirst>
-GB_D bool trace_scene(const DevScene& s, float3 o, float3 d, float tmin, float tmax, uint32_t flags,
-                      const AnyCtx& ctx, Hit& best, TraceStats& st) {
-    best.t = tmax;
-    best.u = best.v = 0.0f;
-    best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
-    if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) return false;
-    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
-    TRay r;
-    setup_ray(r, o, d);
-    if (s.has_world) {
-        float tn;
-        if (box_hit(r, s.world_lo.x, s.world_hi.x, s.world_lo.y, s.world_hi.y, s.world_lo.z, s.world_hi.z, tmin,
-                    best.t, tn)) {
-            if (traverse_bvh<kTerminateOnFirst>(s, s.world_root, r, tmin, best, test_alpha, ctx, st, -1))
-                return true;
-        }
-    }
-    if (s.has_tlas) {
+GB_D bool trace_tlas(const DevScene& s, const TRay& r, float3 o, float3 d, float tmin, Hit& best, bool test_alpha,
+                     const AnyCtx& ctx, TraceStats& st) {
+    {
         float tn;
         if (box_hit(r, s.tlas_lo.x, s.tlas_hi.x, s.tlas_lo.y, s.tlas_hi.y, s.tlas_lo.z, s.tlas_hi.z, tmin, best.t,
                     tn)) {
@@ -277,6 +263,29 @@ GB_D bool trace_scene(const DevScene& s, float3 o, float3 d, float tmin, float t
             }
         }
     }
+    return best.inst != 0xFFFFFFFFu;
+}
+
+// Full query: the merged world BVH, then the TLAS over transformed instances.
+template <bool kTerminateOnFirst>
+GB_D bool trace_scene(const DevScene& s, float3 o, float3 d, float tmin, float tmax, uint32_t flags,
+                      const AnyCtx& ctx, Hit& best, TraceStats& st) {
+    best.t = tmax;
+    best.u = best.v = 0.0f;
+    best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
+    if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) return false;
+    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+    TRay r;
+    setup_ray(r, o, d);
+    if (s.has_world) {
+        float tn;
+        if (box_hit(r, s.world_lo.x, s.world_hi.x, s.world_lo.y, s.world_hi.y, s.world_lo.z, s.world_hi.z, tmin,
+                    best.t, tn)) {
+            if (traverse_bvh<kTerminateOnFirst>(s, s.world_root, r, tmin, best, test_alpha, ctx, st, -1))
+                return true;
+        }
+    }
+    if (s.has_tlas) trace_tlas<kTerminateOnFirst>(s, r, o, d, tmin, best, test_alpha, ctx, st);
     return best.inst != 0xFFFFFFFFu;
 }
 

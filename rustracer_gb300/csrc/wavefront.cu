@@ -12,6 +12,7 @@
 // added as (E + C) after the shadow test like RayTracing.rchit:346-349.
 #include "hitgroup.cuh"
 #include "kernels.h"
+#include "persistent.cuh"
 
 namespace gbrt {
 
@@ -95,26 +96,30 @@ __global__ void __launch_bounds__(128) wf_camera(gbrt_ubo ubo, WfParams p) {
 }
 
 // traceRayEXT for the extension queue of bounce b (closest hit).
+template <bool kWide>
 __global__ void __launch_bounds__(128) wf_extend(DevScene s, WfParams p, uint32_t b) {
     const uint32_t n = p.st.counts[kQueue + b];
     const float4* __restrict__ ro = p.st.ray_o[b & 1];
     const float4* __restrict__ rd = p.st.ray_d[b & 1];
     TraceStats ts{0, 0, 0};
-    for (;;) {
-        const uint32_t base = warp_fetch(&p.st.counts[kWorkExt + b]);
-        if (base >= n) break;
-        const uint32_t q = base + lane_id();
-        if (q < n) {
+    world_trace<false, kWide>(
+        s, n, &p.st.counts[kWorkExt + b], p.flags, ts,
+        [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
             const float4 o4 = ro[q], d4 = rd[q];
-            const uint32_t pid = __float_as_uint(d4.w);
             uint32_t pix, x, y, j;
-            path_coords(p, pid, pix, x, y, j);
-            Hit h;
-            const AnyCtx ctx{x, y, p.sample0 + j, b};
-            const bool hit = trace_scene<false>(s, f3(o4), f3(d4), 0.001f, p.tfar, p.flags, ctx, h, ts);
+            path_coords(p, __float_as_uint(d4.w), pix, x, y, j);
+            o = f3(o4);
+            d = f3(d4);
+            tmin = 0.001f;
+            tmax = p.tfar;
+            ctx = AnyCtx{x, y, p.sample0 + j, b};
+        },
+        [&](uint32_t q, bool hit, const Hit& h) {
             p.st.hit[q] = f4(hit ? h.t : -1.0f, h.u, h.v, __uint_as_float(hit ? h.inst : 0xFFFFFFFFu));
             p.st.hit_prim[q] = h.prim;
             if (b == 0 && p.out.primary_hits) {
+                uint32_t pix, x, y, j;
+                path_coords(p, __float_as_uint(rd[q].w), pix, x, y, j);
                 gbrt_hit g;
                 g.t = hit ? h.t : -1.0f;
                 g.u = hit ? h.u : 0.0f;
@@ -124,8 +129,7 @@ __global__ void __launch_bounds__(128) wf_extend(DevScene s, WfParams p, uint32_
                 g.custom_index = hit ? s.inst[h.inst].custom : 0xFFFFFFFFu;
                 p.out.primary_hits[(size_t)pix * p.ns + p.si0 + j] = g;
             }
-        }
-    }
+        });
     const unsigned long long nodes = warp_sum<unsigned long long>(ts.nodes);
     const unsigned long long tris = warp_sum<unsigned long long>(ts.tris);
     uint32_t stat = ts.status;
@@ -239,30 +243,33 @@ __global__ void __launch_bounds__(128) wf_shade(DevScene s, gbrt_ubo ubo, WfPara
 
 // Any-hit shadow rays of bounce b (castShadowRay, RayTracing.rchit:35-59),
 // then the deferred radiance update radiance += tp * (E [+ C if unoccluded]).
+template <bool kWide>
 __global__ void __launch_bounds__(128) wf_shadow(DevScene s, WfParams p, uint32_t b) {
     const uint32_t n = p.st.counts[kShadow + b];
     TraceStats ts{0, 0, 0};
     const uint32_t flags = GBRT_RAY_TERMINATE_ON_FIRST | p.flags;
-    for (;;) {
-        const uint32_t base = warp_fetch(&p.st.counts[kWorkSh + b]);
-        if (base >= n) break;
-        const uint32_t q = base + lane_id();
-        if (q < n) {
-            const float4 o4 = p.st.sh_o[q], d4 = p.st.sh_d[q], e4 = p.st.sh_e[q], c4 = p.st.sh_c[q];
+    world_trace<true, kWide>(
+        s, n, &p.st.counts[kWorkSh + b], flags, ts,
+        [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
+            const float4 o4 = p.st.sh_o[q], d4 = p.st.sh_d[q];
+            uint32_t pix, x, y, j;
+            path_coords(p, __float_as_uint(d4.w), pix, x, y, j);
+            o = f3(o4);
+            d = f3(d4);
+            tmin = 0.1f;
+            tmax = o4.w;
+            ctx = AnyCtx{x, y, p.sample0 + j, b | 0x100u};
+        },
+        [&](uint32_t q, bool occluded, const Hit&) {
+            const float4 d4 = p.st.sh_d[q], e4 = p.st.sh_e[q], c4 = p.st.sh_c[q];
             const float tpz = p.st.sh_tp[q];
             const uint32_t pid = __float_as_uint(d4.w);
-            uint32_t pix, x, y, j;
-            path_coords(p, pid, pix, x, y, j);
-            Hit h;
-            const AnyCtx ctx{x, y, p.sample0 + j, b | 0x100u};
-            const bool occluded = trace_scene<true>(s, f3(o4), f3(d4), 0.1f, o4.w, flags, ctx, h, ts);
             float3 e = f3(e4);
             if (!occluded) e += f3(c4);
-            float4 r = p.st.rad[pid];
+            const float4 r = p.st.rad[pid];
             const float3 rad = f3(r) + f3(e4.w, c4.w, tpz) * e;
             p.st.rad[pid] = f4(rad, r.w);
-        }
-    }
+        });
     const unsigned long long nodes = warp_sum<unsigned long long>(ts.nodes);
     const unsigned long long tris = warp_sum<unsigned long long>(ts.tris);
     uint32_t stat = ts.status;
@@ -332,9 +339,9 @@ cudaError_t grids(Grid& g) {
     if (g.dev == dev) return cudaSuccess;
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend<true>, 128, 0)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<true>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
     g.shadow = sms * (bh > 0 ? bh : 1);
@@ -345,8 +352,50 @@ cudaError_t grids(Grid& g) {
 
 size_t wavefront_bytes_per_path() { return 4 * 16 + 16 + 4 + 4 * 16 + 4 * 16 + 4; }
 
+namespace {
+cudaError_t timer_grow(StageTimer& t, int pairs) {
+    if (pairs <= t.capacity) return cudaSuccess;
+    cudaEvent_t* ev = new cudaEvent_t[2 * pairs];
+    int* stage = new int[pairs];
+    for (int i = 0; i < 2 * t.capacity; ++i) ev[i] = t.ev[i];
+    for (int i = 2 * t.capacity; i < 2 * pairs; ++i) {
+        cudaError_t e = cudaEventCreate(&ev[i]);
+        if (e != cudaSuccess) {
+            for (int k = 2 * t.capacity; k < i; ++k) cudaEventDestroy(ev[k]);
+            delete[] ev;
+            delete[] stage;
+            return e;
+        }
+    }
+    delete[] t.ev;
+    delete[] t.stage;
+    t.ev = ev;
+    t.stage = stage;
+    t.capacity = pairs;
+    return cudaSuccess;
+}
+}  // namespace
+
+void stage_timer_free(StageTimer& t) {
+    for (int i = 0; i < 2 * t.capacity; ++i) cudaEventDestroy(t.ev[i]);
+    delete[] t.ev;
+    delete[] t.stage;
+    t = StageTimer{};
+}
+
+cudaError_t stage_timer_collect(StageTimer& t, double ms[4]) {
+    for (int k = 0; k < 4; ++k) ms[k] = 0.0;
+    for (int i = 0; i < t.used; ++i) {
+        float f = 0.0f;
+        cudaError_t e = cudaEventElapsedTime(&f, t.ev[2 * i], t.ev[2 * i + 1]);
+        if (e != cudaSuccess) return e;
+        ms[t.stage[i]] += f;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, StageTimer* timer) {
     if (ubo.number_of_bounces > kMaxBounces) return cudaErrorInvalidValue;
     cudaError_t e = grids(g_grid);
     if (e != cudaSuccess) return e;
@@ -362,6 +411,21 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
     p.flags = ubo.fully_opaque ? GBRT_RAY_OPAQUE : 0u;
     p.out = out;
     const uint32_t nb = ubo.number_of_bounces;
+    if (timer) {
+        const uint64_t npw0 = npix < st.cap ? npix : st.cap, k0 = st.cap / npw0;
+        const uint64_t waves = ((npix + npw0 - 1) / npw0) * ((ns + k0 - 1) / k0);
+        if ((e = timer_grow(*timer, (int)(waves * (2 + 3 * nb) + 1))) != cudaSuccess) return e;
+        timer->used = 0;
+    }
+    auto tb = [&](int stage) {
+        if (timer) {
+            timer->stage[timer->used] = stage;
+            cudaEventRecord(timer->ev[2 * timer->used], stream);
+        }
+    };
+    auto te = [&]() {
+        if (timer) cudaEventRecord(timer->ev[2 * timer->used++ + 1], stream);
+    };
     // waves: k samples of a pixel range, k * npw <= cap
     for (uint32_t px0 = 0; px0 < npix;) {
         const uint32_t npw = npix - px0 < st.cap ? npix - px0 : st.cap;
@@ -374,19 +438,96 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
             p.si0 = s0;
             p.npaths = k * npw;
             if ((e = cudaMemsetAsync(st.counts, 0, kWfCounters * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+            tb(3);
             wf_camera<<<(p.npaths + 127) / 128, 128, 0, stream>>>(ubo, p);
+            te();
             for (uint32_t b = 0; b < nb; ++b) {
-                wf_extend<<<g_grid.extend, 128, 0, stream>>>(s, p, b);
+                tb(0);
+                if (s.cw_nodes) wf_extend<true><<<g_grid.extend, 128, 0, stream>>>(s, p, b);
+                else wf_extend<false><<<g_grid.extend, 128, 0, stream>>>(s, p, b);
+                te();
+                tb(1);
                 wf_shade<<<g_grid.shade, 128, 0, stream>>>(s, ubo, p, b);
-                wf_shadow<<<g_grid.shadow, 128, 0, stream>>>(s, p, b);
+                te();
+                tb(2);
+                if (s.cw_nodes) wf_shadow<true><<<g_grid.shadow, 128, 0, stream>>>(s, p, b);
+                else wf_shadow<false><<<g_grid.shadow, 128, 0, stream>>>(s, p, b);
+                te();
             }
+            tb(3);
             wf_finish<<<(npw + 127) / 128, 128, 0, stream>>>(p, k);
+            te();
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             s0 += k;
         }
         px0 += npw;
     }
+    tb(3);
     wf_resolve<<<(npix + 127) / 128, 128, 0, stream>>>(ubo, out, st.frame_sum);
+    te();
+    return cudaGetLastError();
+}
+
+}  // namespace gbrt
+
+namespace gbrt {
+
+// traceRayEXT queries (gbrt_trace_rays) through the persistent traversal of
+// the world BVH in the layout the scene carries.
+template <bool kAny, bool kWide>
+__global__ void __launch_bounds__(128) trace_rays_persistent(DevScene s, const gbrt_ray* rays, uint32_t n,
+                                                             uint32_t flags, gbrt_hit* hits, uint32_t* work,
+                                                             DeviceCounters* cnt) {
+    TraceStats ts{0, 0, 0};
+    world_trace<kAny, kWide>(
+        s, n, work, flags, ts,
+        [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
+            const gbrt_ray r = rays[q];
+            o = f3(r.org[0], r.org[1], r.org[2]);
+            d = f3(r.dir[0], r.dir[1], r.dir[2]);
+            tmin = r.tmin;
+            tmax = r.tmax;
+            ctx = AnyCtx{q, 0u, 0u, 0u};
+        },
+        [&](uint32_t q, bool hit, const Hit& h) {
+            gbrt_hit g;
+            g.t = hit ? h.t : -1.0f;
+            g.u = hit ? h.u : 0.0f;
+            g.v = hit ? h.v : 0.0f;
+            g.instance_id = hit ? h.inst : 0xFFFFFFFFu;
+            g.primitive_id = hit ? h.prim : 0xFFFFFFFFu;
+            g.custom_index = hit ? s.inst[h.inst].custom : 0xFFFFFFFFu;
+            hits[q] = g;
+        });
+    if (cnt) {
+        const unsigned long long nodes = warp_sum<unsigned long long>(ts.nodes);
+        const unsigned long long tris = warp_sum<unsigned long long>(ts.tris);
+        uint32_t stat = ts.status;
+        for (int o = 16; o > 0; o >>= 1) stat |= __shfl_down_sync(0xFFFFFFFFu, stat, o);
+        if ((threadIdx.x & 31u) == 0) {
+            atomicAdd(&cnt->nodes, nodes);
+            atomicAdd(&cnt->tris, tris);
+            if (stat) atomicOr(&cnt->status, stat);
+        }
+    }
+}
+
+cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays, uint32_t n, uint32_t flags,
+                                         gbrt_hit* hits, uint32_t* work, DeviceCounters* cnt, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = grids(g_grid);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+    const uint32_t need = (n + 127) / 128;
+    const uint32_t grid = need < (uint32_t)g_grid.extend ? need : (uint32_t)g_grid.extend;
+    const bool any = flags & GBRT_RAY_TERMINATE_ON_FIRST;
+    if (s.cw_nodes) {
+        if (any) trace_rays_persistent<true, true><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+        else trace_rays_persistent<false, true><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+    } else {
+        if (any) trace_rays_persistent<true, false><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+        else trace_rays_persistent<false, false><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+    }
     return cudaGetLastError();
 }
 

@@ -63,12 +63,13 @@ HIT = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("instance_id", "<u4")
 
 STATS = np.dtype([("rays_total", "<u8"), ("rays_camera", "<u8"), ("rays_extension", "<u8"),
                   ("rays_shadow", "<u8"), ("hits_shaded", "<u8"), ("device_ms", "<f8"),
-                  ("kernel_launches", "<u4"), ("device_status", "<u4")])
+                  ("kernel_launches", "<u4"), ("device_status", "<u4"), ("node_visits", "<u8"),
+                  ("tri_tests", "<u8"), ("stage_ms", "<f8", 4)])
 
 SKIN = np.dtype([("joints", "<f4", (256, 16))])
 
 for _dt, _size in ((VERTEX, 128), (PRIMINFO, 16), (MATERIAL, 256), (LIGHT, 48), (UBO, 324),
-                   (INSTANCE, 64), (GEO_RANGE, 16), (RAY, 32), (HIT, 24), (STATS, 56), (SKIN, 16384)):
+                   (INSTANCE, 64), (GEO_RANGE, 16), (RAY, 32), (HIT, 24), (STATS, 104), (SKIN, 16384)):
     assert _dt.itemsize == _size, (_dt, _dt.itemsize, _size)
 assert MATERIAL.fields["base_color"][1] == 32
 assert MATERIAL.fields["attenuation_color"][1] == 128
