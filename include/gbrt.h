@@ -418,6 +418,67 @@ int gbrt_trace_rays_device(gbrt_scene* scene, const gbrt_ray* d_rays, uint32_t n
 int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices);
 
 /* ------------------------------------------------------------------------ */
+/* Jobs: asynchronous frames with continuous batching                       */
+/* ------------------------------------------------------------------------ */
+/* No reference counterpart: the reference renders one frame at a time from
+ * its render thread (record_raytracing_commands, crates/examples/
+ * gltf_viewer/src/main.rs:244-270).  A job is one gbrt_render_ex call made
+ * asynchronous.  Jobs on a context are traced by one scheduler thread on the
+ * context's stream in waves of at most 2^21 paths; each wave packs segments
+ * (a pixel range x a sample range) of up to 32 admitted jobs, possibly of
+ * different scenes, so jobs join and leave the running batch at wave
+ * boundaries.  A job's image and accumulation are bit-identical to the same
+ * frame rendered alone by gbrt_render_ex in wavefront mode.
+ *
+ * Admission: a queued job is admitted when fewer than 32 jobs are active and
+ * its device memory (20 B per pixel: frame sum + image) fits the HBM budget
+ * still free; admission is in submission order.  Among admitted jobs, waves
+ * are filled shortest-remaining-work first (GBRT_JOB_POLICY_SRPT, default)
+ * or in submission order (GBRT_JOB_POLICY_FIFO).
+ *
+ * While a context has unfinished jobs, its synchronous calls that use the
+ * stream (render, trace, builds, skinning, lights, skybox) return
+ * GBRT_E_BUSY, and a scene or accumulation buffer used by an unfinished job
+ * cannot be destroyed or reset.  A skinned scene is animated by jobs that
+ * carry skins: the scheduler admits such a job once no active job uses that
+ * scene, then skins it and rebuilds its BVH before the job's first wave. */
+#define GBRT_JOB_QUEUED   0u
+#define GBRT_JOB_RUNNING  1u
+#define GBRT_JOB_DONE     2u
+#define GBRT_JOB_POLICY_SRPT 0u
+#define GBRT_JOB_POLICY_FIFO 1u
+
+typedef struct gbrt_job_desc {
+    gbrt_scene* scene;
+    const gbrt_ubo* ubo;          /* copied at submit */
+    gbrt_accum* accum;            /* image size = the accumulation buffer's */
+    uint8_t* out_rgba8;           /* host image written when the job finishes, may be NULL */
+    const gbrt_skin_raw* skins;   /* non-NULL: skin the scene (copied at submit) before the job */
+    uint32_t nskin;
+    uint32_t flags;               /* reserved, 0 */
+} gbrt_job_desc;
+
+typedef struct gbrt_job_info {
+    uint32_t state;      /* GBRT_JOB_* */
+    int32_t status;      /* GBRT_OK or the error of a finished job */
+    double queue_ms;     /* submit -> admitted */
+    double latency_ms;   /* submit -> finished (image on the host) */
+    gbrt_stats stats;    /* the job's rays, shaded hits, node visits; device_ms = admitted -> finished */
+} gbrt_job_info;
+
+/* Queues a job; *job_id gets its handle.  Never blocks on the GPU. */
+int gbrt_job_submit(gbrt_ctx* ctx, const gbrt_job_desc* desc, uint64_t* job_id);
+/* GBRT_OK and the job's info once it has finished (the handle is then
+ * released: a later poll of the same id is GBRT_E_INVALID); GBRT_E_BUSY
+ * with the current state while it is queued or running. */
+int gbrt_job_poll(gbrt_ctx* ctx, uint64_t job_id, gbrt_job_info* info);
+/* Like poll, but waits up to timeout_ms (0xFFFFFFFF = no limit). */
+int gbrt_job_wait(gbrt_ctx* ctx, uint64_t job_id, uint32_t timeout_ms, gbrt_job_info* info);
+/* HBM budget for admitted jobs (0 = the device memory free when the first job
+ * is submitted, minus 1 GiB) and the wave-filling policy. */
+int gbrt_jobs_configure(gbrt_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t policy);
+
+/* ------------------------------------------------------------------------ */
 /* Device memory helpers (for callers without a CUDA runtime of their own)  */
 /* ------------------------------------------------------------------------ */
 int gbrt_device_alloc(gbrt_ctx* ctx, uint64_t bytes, void** d_ptr);

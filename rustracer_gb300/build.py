@@ -51,6 +51,7 @@ def build(force=False, verbose=False, ptxas_info=False):
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
+    extra += os.environ.get("GBRT_NVCC_FLAGS", "").split()  # e.g. -DGBRT_TRACE_MINB=4 for tuning sweeps
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")

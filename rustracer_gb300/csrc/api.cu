@@ -13,9 +13,10 @@
 #include <string>
 #include <vector>
 
-#include "kernels.h"
+#include "api_internal.h"
 
 using namespace gbrt;
+using namespace gbrt_host;
 
 static_assert(sizeof(gbrt_vertex) == 128, "Vertex is 128 B (geometry.rs:10-22)");
 static_assert(sizeof(gbrt_priminfo) == 16, "PrimInfo is 16 B");
@@ -29,85 +30,13 @@ static_assert(sizeof(gbrt_instance) == 64, "VkAccelerationStructureInstanceKHR i
 static_assert(sizeof(gbrt_skin_raw) == 16384, "Skin is 256 mat4");
 static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records");
 static_assert(sizeof(gbrt_stats) == 104, "stats record");
+static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 48, "job records");
 
 namespace {
-
 thread_local std::string g_create_error;
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    cudaError_t alloc(size_t n) {
-        if (n == bytes && p) return cudaSuccess;
-        release();
-        if (n == 0) return cudaSuccess;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        else p = nullptr;
-        return e;
-    }
-    // grows only
-    cudaError_t reserve(size_t n) { return n <= bytes ? cudaSuccess : alloc(n); }
-    template <class T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
 }  // namespace
 
-struct gbrt_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tb0 = nullptr, tb1 = nullptr;
-    std::string err;
-    DevBuf counters;
-    DevBuf trace_work;  // fetch cursor of the persistent ray-query kernel
-    DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
-    DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums
-    WfState wf{};
-    StageTimer timer;
-    std::mutex mu;
-};
-
-struct gbrt_scene {
-    gbrt_ctx* ctx = nullptr;
-    uint32_t nv = 0, ni = 0, ngeo = 0, nmat = 0, ntex = 0;
-    DevBuf vertices, base_vertices, indices, prims, mats, tex_descs, dlights, plights, sky, skins;
-    std::vector<DevBuf*> tex_data;
-    std::vector<gbrt_priminfo> h_prims;
-    std::vector<uint32_t> h_indices;     // for range validation
-    std::vector<gbrt_geo_range> ranges;  // by geo id
-    std::vector<uint8_t> has_range;
-    std::vector<gbrt_instance> instances;
-    uint32_t nd = 0, np = 0, sky_size = 0;
-    bool skinned = false;
-    bool all_opaque = true;
-    // acceleration structures
-    DevBuf nodes, tris, inst, items;
-    DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
-    uint32_t cw_count = 0;
-    bool built = false;
-    DevScene view{};
-    ~gbrt_scene() {
-        for (DevBuf* b : tex_data) delete b;
-    }
-};
-
-struct gbrt_accum {
-    gbrt_ctx* ctx = nullptr;
-    uint32_t w = 0, h = 0;
-    DevBuf buf;
-};
-
-namespace {
+namespace gbrt_host {
 
 int fail(gbrt_ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
@@ -119,25 +48,6 @@ int cuda_fail(gbrt_ctx* c, cudaError_t e, const char* what) {
     return fail(c, e == cudaErrorMemoryAllocation ? GBRT_E_OOM : GBRT_E_CUDA,
                 std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
 }
-#define CU(ctx, x, what)                                   \
-    do {                                                   \
-        cudaError_t e_ = (x);                              \
-        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 // World-to-object transform: adjugate inverse of the 3x3 part in double and
 // translation -R^-1 t, each rounded once to float (the oracle computes the
 // same expression).
@@ -173,7 +83,8 @@ cudaError_t upload(DevBuf& b, const T* src, size_t n, cudaStream_t st) {
 cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t f4 = al((size_t)cap * sizeof(float4)), u1 = al((size_t)cap * 4);
-    const size_t bytes = 13 * f4 + 2 * u1 + al(kWfCounters * sizeof(uint32_t));
+    const size_t counts = al((size_t)kMaxWaveJobs * kWfCounters * sizeof(uint32_t));
+    const size_t bytes = 13 * f4 + 2 * u1 + counts;
     if (c->wf.cap < cap || c->wf_mem.bytes < bytes) {
         cudaError_t e = c->wf_mem.alloc(bytes);
         if (e != cudaSuccess) {
@@ -198,7 +109,7 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
         w.sh_c = (float4*)take(f4);
         w.hit_prim = (uint32_t*)take(u1);
         w.sh_tp = (float*)take(u1);
-        w.counts = (uint32_t*)take(al(kWfCounters * sizeof(uint32_t)));
+        w.counts = (uint32_t*)take(counts);
         w.cap = cap;
     }
     cudaError_t e = c->wf_frame.reserve(npix * sizeof(float4));
@@ -391,7 +302,24 @@ void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t la
     for (int k = 0; k < 4; ++k) st->stage_ms[k] = 0.0;
 }
 
-}  // namespace
+int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin) {
+    gbrt_ctx* c = s->ctx;
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    if (!s->skinned) {  // keep the bind-pose vertices (the reference's vertex_buffer)
+        CU(c, s->base_vertices.alloc(s->vertices.bytes), "cudaMalloc(base vertices)");
+        CU(c, cudaMemcpyAsync(s->base_vertices.p, s->vertices.p, s->vertices.bytes, cudaMemcpyDeviceToDevice, st),
+           "copy");
+        s->skinned = true;
+    }
+    CU(c, upload(s->skins, skins, nskin, st), "upload(skins)");
+    CU(c, launch_skinning(s->base_vertices.as<gbrt_vertex>(), s->vertices.as<gbrt_vertex>(), s->nv,
+                          s->skins.as<gbrt_skin_raw>(), nskin, st),
+       "skinning");
+    return build_all(s);
+}
+
+}  // namespace gbrt_host
 
 extern "C" {
 
@@ -432,12 +360,14 @@ int gbrt_ctx_create(int device, gbrt_ctx** out) {
     }
     if ((e = init_render_constants(lut)) != cudaSuccess) return bail(e, "constants");
     if ((e = init_wavefront_constants(lut)) != cudaSuccess) return bail(e, "constants");
+    if ((e = init_wave_multi_constants(lut)) != cudaSuccess) return bail(e, "constants");
     *out = c;
     return GBRT_OK;
 }
 
 int gbrt_ctx_destroy(gbrt_ctx* c) {
     if (!c) return GBRT_OK;
+    jobs_shutdown(c);  // finishes the queued jobs, joins the scheduler
     {
         DeviceGuard g(c->device);
         if (c->stream) cudaStreamSynchronize(c->stream);
@@ -451,6 +381,7 @@ int gbrt_ctx_destroy(gbrt_ctx* c) {
         c->wf_mem.release();
         c->wf_frame.release();
         stage_timer_free(c->timer);
+        wave_ring_free(c->ring);
         if (c->ev0) cudaEventDestroy(c->ev0);
         if (c->ev1) cudaEventDestroy(c->ev1);
         if (c->tb0) cudaEventDestroy(c->tb0);
@@ -544,6 +475,7 @@ int gbrt_scene_create(gbrt_ctx* c, const gbrt_vertex* v, uint32_t nv, const uint
 
 int gbrt_scene_destroy(gbrt_scene* s) {
     if (!s) return GBRT_OK;
+    if (s->jobs_pending.load()) return fail(s->ctx, GBRT_E_BUSY, "jobs that render this scene are unfinished");
     DeviceGuard g(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     delete s;
@@ -553,6 +485,7 @@ int gbrt_scene_destroy(gbrt_scene* s) {
 int gbrt_blas_build(gbrt_scene* s, const gbrt_geo_range* r, uint32_t n, uint32_t flags) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && !r) return fail(c, GBRT_E_INVALID, "ranges is NULL");
     if (flags != 0) return fail(c, GBRT_E_INVALID, "flags must be 0");
     for (uint32_t i = 0; i < n; ++i) {
@@ -575,6 +508,7 @@ int gbrt_blas_build(gbrt_scene* s, const gbrt_geo_range* r, uint32_t n, uint32_t
 
 int gbrt_tlas_build(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
     if (!s) return GBRT_E_INVALID;
+    if (jobs_outstanding(s->ctx)) return fail(s->ctx, GBRT_E_BUSY, "jobs are running on this context");
     if (n && !in) return fail(s->ctx, GBRT_E_INVALID, "instances is NULL");
     DeviceGuard g(s->ctx->device);
     s->instances.assign(in, in + n);
@@ -592,24 +526,14 @@ int gbrt_skin_and_refit(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nski
     gbrt_ctx* c = s->ctx;
     if (nskin && !skins) return fail(c, GBRT_E_INVALID, "skins is NULL");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS before skinning");
-    DeviceGuard g(c->device);
-    cudaStream_t st = c->stream;
-    if (!s->skinned) {  // keep the bind-pose vertices (the reference's vertex_buffer)
-        CU(c, s->base_vertices.alloc(s->vertices.bytes), "cudaMalloc(base vertices)");
-        CU(c, cudaMemcpyAsync(s->base_vertices.p, s->vertices.p, s->vertices.bytes, cudaMemcpyDeviceToDevice, st),
-           "copy");
-        s->skinned = true;
-    }
-    CU(c, upload(s->skins, skins, nskin, st), "upload(skins)");
-    CU(c, launch_skinning(s->base_vertices.as<gbrt_vertex>(), s->vertices.as<gbrt_vertex>(), s->nv,
-                          s->skins.as<gbrt_skin_raw>(), nskin, st),
-       "skinning");
-    return build_all(s);
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
+    return skin_scene(s, skins, nskin);
 }
 
 int gbrt_lights_set(gbrt_scene* s, const gbrt_light_raw* d, uint32_t nd, const gbrt_light_raw* p, uint32_t np) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if ((nd && !d) || (np && !p)) return fail(c, GBRT_E_INVALID, "lights pointer is NULL");
     DeviceGuard g(c->device);
     CU(c, upload(s->dlights, d, nd, c->stream), "upload(dlights)");
@@ -624,6 +548,7 @@ int gbrt_lights_set(gbrt_scene* s, const gbrt_light_raw* d, uint32_t nd, const g
 int gbrt_skybox_set(gbrt_scene* s, uint32_t size, const uint8_t* faces) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     DeviceGuard g(c->device);
     if (!faces || size == 0) {
         s->sky.release();
@@ -659,6 +584,7 @@ int gbrt_accum_create(gbrt_ctx* c, uint32_t w, uint32_t h, gbrt_accum** out) {
 
 int gbrt_accum_reset(gbrt_accum* a) {
     if (!a) return GBRT_E_INVALID;
+    if (a->jobs_pending.load()) return fail(a->ctx, GBRT_E_BUSY, "a job writes this accumulation buffer");
     DeviceGuard g(a->ctx->device);
     CU(a->ctx, cudaMemsetAsync(a->buf.p, 0, a->buf.bytes, a->ctx->stream), "memset");
     return GBRT_OK;
@@ -666,6 +592,7 @@ int gbrt_accum_reset(gbrt_accum* a) {
 
 int gbrt_accum_download(gbrt_accum* a, float* dst) {
     if (!a || !dst) return a ? fail(a->ctx, GBRT_E_INVALID, "dst is NULL") : GBRT_E_INVALID;
+    if (a->jobs_pending.load()) return fail(a->ctx, GBRT_E_BUSY, "a job writes this accumulation buffer");
     DeviceGuard g(a->ctx->device);
     CU(a->ctx, cudaMemcpyAsync(dst, a->buf.p, a->buf.bytes, cudaMemcpyDeviceToHost, a->ctx->stream), "download");
     CU(a->ctx, cudaStreamSynchronize(a->ctx->stream), "sync");
@@ -674,6 +601,7 @@ int gbrt_accum_download(gbrt_accum* a, float* dst) {
 
 int gbrt_accum_destroy(gbrt_accum* a) {
     if (!a) return GBRT_OK;
+    if (a->jobs_pending.load()) return fail(a->ctx, GBRT_E_BUSY, "a job writes this accumulation buffer");
     DeviceGuard g(a->ctx->device);
     cudaStreamSynchronize(a->ctx->stream);
     delete a;
@@ -684,6 +612,7 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
                    const gbrt_render_opts* opts) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (!ubo || !acc) return fail(c, GBRT_E_INVALID, "ubo or accumulation buffer is NULL");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before rendering");
     if (acc->ctx != c) return fail(c, GBRT_E_INVALID, "accumulation buffer belongs to another context");
@@ -761,6 +690,7 @@ int gbrt_trace_rays_device(gbrt_scene* s, const gbrt_ray* d_rays, uint32_t n, ui
     gbrt_ctx* c = s->ctx;
     if (n && (!d_rays || !d_hits)) return fail(c, GBRT_E_INVALID, "rays or hits is NULL");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tracing");
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     DeviceGuard g(c->device);
     CU(c, launch_trace_rays_persistent(s->view, d_rays, n, flags, d_hits, c->trace_work.as<uint32_t>(), nullptr,
                                        c->stream),
@@ -772,6 +702,7 @@ int gbrt_trace_rays(gbrt_scene* s, const gbrt_ray* rays, uint32_t n, uint32_t fl
                     gbrt_stats* stats) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && (!rays || !hits)) return fail(c, GBRT_E_INVALID, "rays or hits is NULL");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tracing");
     DeviceGuard g(c->device);

@@ -1,0 +1,137 @@
+// api_internal.h -- host-side objects behind the C ABI handles, shared by
+// api.cu (the entry points) and jobs.cu (the job scheduler).
+#pragma once
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+using gbrt::DevScene;
+using gbrt::DeviceCounters;
+using gbrt::StageTimer;
+using gbrt::WaveRing;
+using gbrt::WfState;
+
+namespace gbrt_host {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        if (n == bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    // grows only
+    cudaError_t reserve(size_t n) { return n <= bytes ? cudaSuccess : alloc(n); }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+
+struct JobQueue;  // jobs.cu
+
+}  // namespace gbrt_host
+
+struct gbrt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, tb0 = nullptr, tb1 = nullptr;
+    std::string err;
+    gbrt_host::DevBuf counters;
+    gbrt_host::DevBuf trace_work;  // fetch cursor of the persistent ray-query kernel
+    gbrt_host::DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
+    gbrt_host::DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums
+    WfState wf{};
+    WaveRing ring;
+    StageTimer timer;
+    std::mutex mu;
+    gbrt_host::JobQueue* jobs = nullptr;  // created by the first gbrt_job_submit
+    uint64_t jobs_budget = 0;             // gbrt_jobs_configure before the first job
+    uint32_t jobs_policy = 0;
+};
+
+struct gbrt_scene {
+    gbrt_ctx* ctx = nullptr;
+    uint32_t nv = 0, ni = 0, ngeo = 0, nmat = 0, ntex = 0;
+    gbrt_host::DevBuf vertices, base_vertices, indices, prims, mats, tex_descs, dlights, plights, sky, skins;
+    std::vector<gbrt_host::DevBuf*> tex_data;
+    std::vector<gbrt_priminfo> h_prims;
+    std::vector<uint32_t> h_indices;     // for range validation
+    std::vector<gbrt_geo_range> ranges;  // by geo id
+    std::vector<uint8_t> has_range;
+    std::vector<gbrt_instance> instances;
+    uint32_t nd = 0, np = 0, sky_size = 0;
+    bool skinned = false;
+    bool all_opaque = true;
+    // acceleration structures
+    gbrt_host::DevBuf nodes, tris, inst, items;
+    gbrt_host::DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
+    uint32_t cw_count = 0;
+    bool built = false;
+    std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene
+    DevScene view{};
+    ~gbrt_scene() {
+        for (gbrt_host::DevBuf* b : tex_data) delete b;
+    }
+};
+
+struct gbrt_accum {
+    gbrt_ctx* ctx = nullptr;
+    uint32_t w = 0, h = 0;
+    std::atomic<uint32_t> jobs_pending{0};  // unfinished jobs that write this buffer
+    gbrt_host::DevBuf buf;
+};
+
+namespace gbrt_host {
+
+int fail(gbrt_ctx* c, int code, const std::string& msg);
+int cuda_fail(gbrt_ctx* c, cudaError_t e, const char* what);
+#define CU(ctx, x, what)                                        \
+    do {                                                        \
+        cudaError_t e_ = (x);                                   \
+        if (e_ != cudaSuccess) return gbrt_host::cuda_fail(ctx, e_, what); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Sizes the wavefront buffers for `cap` paths and `npix` pixels (grow only).
+cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix);
+// Rebuilds the world BVH, BLASes and TLAS of a scene from its current vertices.
+int build_all(gbrt_scene* s);
+// Linear-blend skinning of the scene's bind-pose vertices, then build_all.
+int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin);
+void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t launches);
+
+// jobs.cu: stops the scheduler thread after the queued jobs (ctx destroy).
+void jobs_shutdown(gbrt_ctx* c);
+// Jobs submitted and not yet finished on this context.
+uint32_t jobs_outstanding(const gbrt_ctx* c);
+
+}  // namespace gbrt_host

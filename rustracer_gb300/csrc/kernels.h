@@ -21,11 +21,16 @@ struct RenderOut {
 };
 
 // wavefront.cu: device buffers of the wavefront path tracer, `cap` paths.
+// Each job of a wave owns kWfCounters queue lengths and fetch cursors.
 constexpr int kWfCounters = 128;
+constexpr uint32_t kPidBits = 21;                    // path id bits of a queue entry
+constexpr uint32_t kMaxWavePaths = 1u << kPidBits;   // paths per wave
+constexpr int kMaxWaveJobs = 32;                     // jobs sharing one wave
+constexpr int kMaxWaveSegs = 256;                    // (pixel range x sample range) pieces per wave
 struct WfState {
     uint32_t cap;
     float4* ray_o[2];   // extension queues (ping-pong): origin
-    float4* ray_d[2];   //   direction, path id in .w
+    float4* ray_d[2];   //   direction, path id | segment << kPidBits in .w
     float4* hit;        // t, u, v, instance id
     uint32_t* hit_prim;
     float4* tp;         // per path: throughput, Ray.t
@@ -37,9 +42,48 @@ struct WfState {
     float4* sh_e;       //   emission E, throughput.x
     float4* sh_c;       //   NEE term C, throughput.y
     float* sh_tp;       //   throughput.z
-    uint32_t* counts;   // kWfCounters queue lengths and fetch cursors
-    float4* frame_sum;  // per pixel: sum of the frame's samples, last Ray.t
+    uint32_t* counts;   // kMaxWaveJobs * kWfCounters queue lengths and fetch cursors
+    float4* frame_sum;  // per pixel: sum of the frame's samples, last Ray.t (single-frame renders)
 };
+
+// One job of a wave: a scene, its UBO and its outputs.  The job's paths are
+// the contiguous range [path0, path0 + npaths) of the wave; its queues live
+// at the same offsets of the wave's queue arrays.
+struct WaveJob {
+    DevScene s;
+    gbrt_ubo ubo;
+    RenderOut out;
+    float4* frame_sum;  // per pixel of the job's image
+    uint32_t ns;        // samples of the frame (stride of the per-sample outputs)
+    uint32_t flags;     // GBRT_RAY_OPAQUE when the UBO says fully_opaque
+    float tfar;
+    uint32_t path0, npaths;
+};
+// k samples [sample0, sample0 + k) of the pixels [px0, px0 + npw) of a job;
+// path path0 + j * npw + i is sample j of pixel px0 + i.
+struct WaveSeg {
+    uint32_t path0, job, px0, npw, sample0, si0, k, fin0;  // fin0: first thread of wf_finish
+};
+struct WaveDesc {
+    uint32_t njobs, nsegs, npaths, nfin, nb;
+    // per stage (extend, shade, shadow): first block of every job, [njobs] = grid size
+    uint32_t blk[3][kMaxWaveJobs + 1];
+    WaveJob jobs[kMaxWaveJobs];
+    WaveSeg segs[kMaxWaveSegs];
+};
+// Pinned host copies of wave descriptors, reused round-robin; slot i may be
+// rewritten once ev[i] (recorded after its upload) has completed.
+struct WaveRing {
+    static constexpr int kSlots = 4;
+    WaveDesc* host = nullptr;
+    cudaEvent_t ev[kSlots] = {};
+    int next = 0;
+};
+cudaError_t wave_ring_init(WaveRing& r);
+void wave_ring_free(WaveRing& r);
+// Waits until the next slot is free and returns it for filling.
+cudaError_t wave_acquire(WaveRing& r, WaveDesc** slot);
+
 // CUDA-event pairs around every wavefront launch, grouped by stage
 // (0 extend, 1 shade, 2 shadow, 3 other).  Events are created on demand and
 // reused across frames.
@@ -50,6 +94,18 @@ struct StageTimer {
 };
 size_t wavefront_bytes_per_path();
 cudaError_t init_wavefront_constants(const float* srgb_lut);
+cudaError_t init_wave_multi_constants(const float* srgb_lut);
+// Grows a timer to hold `pairs` event pairs, keeping the pairs recorded so far.
+cudaError_t stage_timer_reserve(StageTimer& t, int pairs);
+// Fills the per-stage block partition of `w` (blocks in proportion to each
+// job's paths, at least one) for the current device.
+cudaError_t wave_partition(WaveDesc& w);
+// Uploads the slot wave_acquire returned and launches one wave: camera, `w.nb` x
+// (extend, shade, shadow), finish.  Launch count: 2 + 3 * w.nb.
+cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, StageTimer* timer);
+// Accumulate + tone map of one finished frame (rgen:132-166).
+cudaError_t launch_resolve(const gbrt_ubo& ubo, const RenderOut& out, const float4* frame_sum, cudaStream_t stream);
+// A whole frame of one scene: waves of at most st.cap paths, then resolve.
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
                              cudaStream_t stream, StageTimer* timer = nullptr);
 // Ray queries through the persistent world traversal (8-wide when built);

@@ -1,0 +1,330 @@
+// wavefront.cuh — device code of the wavefront path tracer, shared by the
+// single-frame kernels (wavefront.cu: the wave is one job and one segment,
+// passed as a kernel parameter) and the batched kernels (wave_multi.cu: up to
+// kMaxWaveJobs jobs and kMaxWaveSegs segments in constant memory).
+//
+// A wave is traced as camera -> for each bounce { extend (closest hit) ->
+// shade (closest-hit / miss shaders, Russian roulette, next ray, NEE shadow
+// record) -> shadow (any-hit) } -> finish (per-pixel sums in sample order).
+// Each stage is a small kernel, so the instruction working set fits the cache
+// and lanes of a warp run the same stage; queues between stages are compacted
+// with warp ballots (one atomic per warp).  Results are bit-identical to the
+// megakernel: the same device functions run in the same order per path, the
+// NEE term is added as (E + C) after the shadow test like
+// RayTracing.rchit:346-349.
+//
+// A wave view W gives the kernels: block_job(stage) (the job a block serves),
+// blk0 / nblk (that job's blocks), job(j), seg(i), seg_of_path(pid),
+// seg_of_fin(i), npaths(), nfin().
+#pragma once
+#include "hitgroup.cuh"
+#include "kernels.h"
+#include "persistent.cuh"
+
+// Resident 128-thread blocks per SM the traversal kernels (extend, shadow)
+// are compiled for: 5 gives them 96 registers, enough to keep the traversal
+// state and the 8-wide node decode out of local memory, at 20 warps per SM.
+#ifndef GBRT_TRACE_MINB
+#define GBRT_TRACE_MINB 5
+#endif
+
+namespace gbrt {
+
+GB_D uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated queue append: every lane of the warp calls it; lanes with
+// want == true get consecutive slots.
+GB_D uint32_t warp_append(uint32_t* counter, bool want) {
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, want);
+    uint32_t base = 0;
+    if (lane_id() == 0 && mask) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    return base + __popc(mask & ((1u << lane_id()) - 1u));
+}
+
+template <class T>
+GB_D T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// Counter slots of one job inside WfState::counts (reset at the start of
+// every wave).
+constexpr int kQueue = 0;     // [kQueue + b]: extension-queue length at bounce b
+constexpr int kShadow = 32;   // [kShadow + b]: shadow-queue length at bounce b
+constexpr int kWorkExt = 64;  // [kWorkExt + b]: fetch cursor of extend(b)
+constexpr int kWorkSh = 96;   // [kWorkSh + b]: fetch cursor of shadow(b)
+constexpr int kMaxBounces = 31;
+constexpr uint32_t kPidMask = kMaxWavePaths - 1u;
+
+struct PathXY {
+    uint32_t pid, pix, x, y, j;  // wave path, pixel, coordinates, sample within the segment
+    const WaveSeg* sg;
+};
+
+// Decodes a queue word (path id | segment << kPidBits) of a job with image width W.
+template <class Wv>
+GB_D PathXY decode_path(const Wv& w, uint32_t word, uint32_t W) {
+    PathXY r;
+    r.pid = word & kPidMask;
+    r.sg = &w.seg(word >> kPidBits);
+    const uint32_t local = r.pid - r.sg->path0;
+    r.j = local / r.sg->npw;
+    r.pix = r.sg->px0 + (local - r.j * r.sg->npw);
+    r.y = r.pix / W;
+    r.x = r.pix - r.y * W;
+    return r;
+}
+
+GB_D void flush_trace_stats(const TraceStats& ts, DeviceCounters* c) {
+    const unsigned long long nodes = warp_sum<unsigned long long>(ts.nodes);
+    const unsigned long long tris = warp_sum<unsigned long long>(ts.tris);
+    uint32_t stat = ts.status;
+    for (int o = 16; o > 0; o >>= 1) stat |= __shfl_down_sync(0xFFFFFFFFu, stat, o);
+    if (lane_id() == 0) {
+        atomicAdd(&c->nodes, nodes);
+        atomicAdd(&c->tris, tris);
+        if (stat) atomicOr(&c->status, stat);
+    }
+}
+
+// rgen:32-80 for every path of the wave: seeds (D1), camera ray, path state.
+// Job j's first queue is its paths in order, at the paths' own positions.
+template <class Wv>
+GB_D void camera_body(const Wv& w, const WfState& st) {
+    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pid >= w.npaths()) return;
+    const uint32_t si = w.seg_of_path(pid);
+    const WaveSeg& sg = w.seg(si);
+    const WaveJob& J = w.job(sg.job);
+    if (pid == J.path0) st.counts[sg.job * kWfCounters + kQueue] = J.npaths;
+    const uint32_t W = J.out.width;
+    const uint32_t local = pid - sg.path0, j = local / sg.npw, pix = sg.px0 + (local - j * sg.npw);
+    const uint32_t y = pix / W, x = pix - y * W;
+    const uint32_t sample = sg.sample0 + j;
+    uint32_t seed = tea16(tea16(x, y), sample);
+    uint4 rng = make_uint4(x, y, sample, 0u);
+    float3 o, d;
+    float tfar;
+    camera_ray(J.ubo, x, y, W, J.out.height, rng, seed, o, d, tfar);
+    st.ray_o[0][pid] = f4(o, 0.0f);
+    st.ray_d[0][pid] = f4(d, __uint_as_float(pid | si << kPidBits));
+    st.tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);                   // throughput, Ray.t = 0
+    st.rad[pid] = f4(0.0f, 0.0f, 0.0f, -1.0f);                 // radiance, volume_dis = -1
+    st.hp[pid] = f4(0.0f, 0.0f, 0.0f, __uint_as_float(seed));  // hitPoint, RandomSeed
+    st.rng[pid] = make_uint4(rng.w, 0u, tea16(sample, 0x9E3779B9u), 0u);
+}
+
+// traceRayEXT for the extension queue of bounce b (closest hit).
+template <bool kWide, class Wv>
+GB_D void extend_body(const Wv& w, const WfState& st, uint32_t b) {
+    const uint32_t jb = w.block_job(0);
+    const WaveJob& J = w.job(jb);
+    uint32_t* cnt = st.counts + jb * kWfCounters;
+    const uint32_t n = cnt[kQueue + b], R = J.path0;
+    const float4* __restrict__ ro = st.ray_o[b & 1] + R;
+    const float4* __restrict__ rd = st.ray_d[b & 1] + R;
+    TraceStats ts{0, 0, 0};
+    world_trace<false, kWide>(
+        J.s, n, &cnt[kWorkExt + b], J.flags, ts,
+        [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
+            const float4 o4 = ro[q], d4 = rd[q];
+            const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
+            o = f3(o4);
+            d = f3(d4);
+            tmin = 0.001f;
+            tmax = J.tfar;
+            ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b};
+        },
+        [&](uint32_t q, bool hit, const Hit& h) {
+            st.hit[R + q] = f4(hit ? h.t : -1.0f, h.u, h.v, __uint_as_float(hit ? h.inst : 0xFFFFFFFFu));
+            st.hit_prim[R + q] = h.prim;
+            if (b == 0 && J.out.primary_hits) {
+                const PathXY P = decode_path(w, __float_as_uint(rd[q].w), J.out.width);
+                gbrt_hit g;
+                g.t = hit ? h.t : -1.0f;
+                g.u = hit ? h.u : 0.0f;
+                g.v = hit ? h.v : 0.0f;
+                g.instance_id = hit ? h.inst : 0xFFFFFFFFu;
+                g.primitive_id = hit ? h.prim : 0xFFFFFFFFu;
+                g.custom_index = hit ? J.s.inst[h.inst].custom : 0xFFFFFFFFu;
+                J.out.primary_hits[(size_t)P.pix * J.ns + P.sg->si0 + P.j] = g;
+            }
+        });
+    flush_trace_stats(ts, J.out.counters);
+    if (blockIdx.x == w.blk0(0, jb) && threadIdx.x == 0) {
+        if (b == 0) atomicAdd(&J.out.counters->camera, (unsigned long long)n);
+        else atomicAdd(&J.out.counters->extension, (unsigned long long)n);
+    }
+}
+
+// Closest-hit / miss shading and the rest of rgen's bounce loop
+// (RayTracing.rgen:94-128) for the extension queue of bounce b.
+template <class Wv>
+GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b) {
+    const uint32_t jb = w.block_job(1);
+    const WaveJob& J = w.job(jb);
+    const DevScene& s = J.s;
+    const gbrt_ubo& ubo = J.ubo;
+    uint32_t* cnt = st.counts + jb * kWfCounters;
+    const uint32_t n = cnt[kQueue + b], R = J.path0;
+    const float4* __restrict__ rd = st.ray_d[b & 1] + R;
+    float4* no = st.ray_o[(b + 1) & 1] + R;
+    float4* nd = st.ray_d[(b + 1) & 1] + R;
+    const uint32_t nb = ubo.number_of_bounces;
+    PathStats ps{0, 0, 0, 0, 0};
+    const uint32_t blk0 = w.blk0(1, jb), nblk = w.nblk(1, jb);
+    const uint32_t stride = nblk * blockDim.x;
+    for (uint32_t base = (blockIdx.x - blk0) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t q = base + lane_id();
+        const bool active = q < n;
+        bool cont = false, shadow = false;
+        float3 nxt_o = f3(0.0f), nxt_d = f3(0.0f), so = f3(0.0f), sd = f3(0.0f), sc = f3(0.0f), se = f3(0.0f);
+        float3 tp_before = f3(0.0f);
+        float stmax = 0.0f;
+        uint32_t word = 0;
+        if (active) {
+            const float4 d4 = rd[q];
+            const float3 d = f3(d4);
+            word = __float_as_uint(d4.w);
+            const PathXY P = decode_path(w, word, J.out.width);
+            const uint32_t pid = P.pid;
+            const float4 h4 = st.hit[R + q];
+            const float4 tp4 = st.tp[pid], rad4 = st.rad[pid], hp4 = st.hp[pid];
+            uint4 rg = st.rng[pid];
+            Payload Rp;
+            Rp.hitValue = Rp.scatterDir = Rp.emittance = f3(0.0f);
+            Rp.needScatter = 0;
+            Rp.hitPoint = f3(hp4);
+            Rp.RandomSeed = __float_as_uint(hp4.w);
+            Rp.t = tp4.w;
+            Rp.volume_dis = rad4.w;
+            Rp.rngState = make_uint4(P.x, P.y, rg.z, rg.y);
+            const uint32_t inst = __float_as_uint(h4.w);
+            if (inst != 0xFFFFFFFFu) {
+                Hit h;
+                h.t = h4.x;
+                h.u = h4.y;
+                h.v = h4.z;
+                h.inst = inst;
+                h.prim = st.hit_prim[R + q];
+                h.bgeo = 0;
+                closest_hit(s, ubo, Rp, h, d, ps, [&](float3 o_, float3 d_, float t_, float3 C) {
+                    shadow = true;
+                    so = o_;
+                    sd = d_;
+                    stmax = t_;
+                    sc = C;
+                });
+            } else {
+                miss_shader(s, ubo, Rp, d);
+            }
+            float3 tp = f3(tp4);
+            float3 rad = f3(rad4);
+            tp_before = tp;
+            se = Rp.emittance;
+            if (!shadow) rad += tp * Rp.emittance;
+            cont = b + 1 != nb;
+            if (cont && b > 3u) {  // Russian roulette, rgen:108-118
+                uint4 prng = make_uint4(P.x, P.y, P.sg->sample0 + P.j, rg.x);
+                const float pr = clampf(luminance(tp), 0.01f, 0.95f);
+                if (pr < pcg_rand(prng)) cont = false;
+                else tp /= pr;
+                rg.x = prng.w;
+            }
+            if (cont) {
+                tp *= Rp.hitValue;
+                if (!Rp.needScatter || Rp.t < 0.0f) cont = false;
+            }
+            st.tp[pid] = f4(tp, Rp.t);
+            st.rad[pid] = f4(rad, Rp.volume_dis);
+            st.hp[pid] = f4(Rp.hitPoint, __uint_as_float(Rp.RandomSeed));
+            st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
+            nxt_o = Rp.hitPoint;
+            nxt_d = Rp.scatterDir;
+        }
+        const uint32_t slot = warp_append(&cnt[kQueue + b + 1], cont);
+        if (cont) {
+            no[slot] = f4(nxt_o, 0.0f);
+            nd[slot] = f4(nxt_d, __uint_as_float(word));
+        }
+        const uint32_t sslot = warp_append(&cnt[kShadow + b], shadow);
+        if (shadow) {
+            st.sh_o[R + sslot] = f4(so, stmax);
+            st.sh_d[R + sslot] = f4(sd, __uint_as_float(word));
+            st.sh_e[R + sslot] = f4(se, tp_before.x);
+            st.sh_c[R + sslot] = f4(sc, tp_before.y);
+            st.sh_tp[R + sslot] = tp_before.z;
+        }
+    }
+    const unsigned long long hs = warp_sum<unsigned long long>(ps.shaded);
+    if (lane_id() == 0 && hs) atomicAdd(&J.out.counters->shaded, hs);
+}
+
+// Any-hit shadow rays of bounce b (castShadowRay, RayTracing.rchit:35-59),
+// then the deferred radiance update radiance += tp * (E [+ C if unoccluded]).
+template <bool kWide, class Wv>
+GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b) {
+    const uint32_t jb = w.block_job(2);
+    const WaveJob& J = w.job(jb);
+    uint32_t* cnt = st.counts + jb * kWfCounters;
+    const uint32_t n = cnt[kShadow + b], R = J.path0;
+    const float4* __restrict__ so = st.sh_o + R;
+    const float4* __restrict__ sd = st.sh_d + R;
+    TraceStats ts{0, 0, 0};
+    const uint32_t flags = GBRT_RAY_TERMINATE_ON_FIRST | J.flags;
+    world_trace<true, kWide>(
+        J.s, n, &cnt[kWorkSh + b], flags, ts,
+        [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
+            const float4 o4 = so[q], d4 = sd[q];
+            const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
+            o = f3(o4);
+            d = f3(d4);
+            tmin = 0.1f;
+            tmax = o4.w;
+            ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b | 0x100u};
+        },
+        [&](uint32_t q, bool occluded, const Hit&) {
+            const float4 d4 = sd[q], e4 = st.sh_e[R + q], c4 = st.sh_c[R + q];
+            const float tpz = st.sh_tp[R + q];
+            const uint32_t pid = __float_as_uint(d4.w) & kPidMask;
+            float3 e = f3(e4);
+            if (!occluded) e += f3(c4);
+            const float4 r = st.rad[pid];
+            const float3 rad = f3(r) + f3(e4.w, c4.w, tpz) * e;
+            st.rad[pid] = f4(rad, r.w);
+        });
+    flush_trace_stats(ts, J.out.counters);
+    if (blockIdx.x == w.blk0(2, jb) && threadIdx.x == 0)
+        atomicAdd(&J.out.counters->shadow, (unsigned long long)n);
+}
+
+// Per pixel of every segment: add its samples' radiance to the job's frame
+// sum in sample order (the megakernel's per-pixel order), keep the last Ray.t.
+template <class Wv>
+GB_D void finish_body(const Wv& w, const WfState& st) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nfin()) return;
+    const WaveSeg& sg = w.seg(w.seg_of_fin(i));
+    const WaveJob& J = w.job(sg.job);
+    const uint32_t li = i - sg.fin0, pix = sg.px0 + li;
+    float4 acc = J.frame_sum[pix];
+    float3 sum = f3(acc);
+    float last_t = acc.w;
+    for (uint32_t j = 0; j < sg.k; ++j) {
+        const uint32_t pid = sg.path0 + li + j * sg.npw;
+        const float3 r = f3(st.rad[pid]);
+        if (J.out.sample_radiance) {
+            float* sr = J.out.sample_radiance + ((size_t)pix * J.ns + sg.si0 + j) * 3;
+            sr[0] = r.x;
+            sr[1] = r.y;
+            sr[2] = r.z;
+        }
+        sum += r;
+        last_t = st.tp[pid].w;
+    }
+    J.frame_sum[pix] = f4(sum, last_t);
+}
+
+}  // namespace gbrt

@@ -57,7 +57,13 @@ SIGNATURES = {
     "gbrt_timer_begin": (i32, [P]),
     "gbrt_timer_end": (i32, [P, C.POINTER(C.c_double)]),
     "gbrt_scene_rebuild_noalloc": (i32, [P, P]),
+    "gbrt_job_submit": (i32, [P, P, C.POINTER(u64)]),
+    "gbrt_job_poll": (i32, [P, u64, P]),
+    "gbrt_job_wait": (i32, [P, u64, u32, P]),
+    "gbrt_jobs_configure": (i32, [P, u64, u32]),
 }
+JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
+POLICY_SRPT, POLICY_FIFO = 0, 1
 NOALLOC_MAX_TRIANGLES = 65536
 
 
@@ -100,6 +106,11 @@ class RenderOpts(C.Structure):
                 ("primary_hits", C.c_void_p)]
 
 
+class JobDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("ubo", C.c_void_p), ("accum", C.c_void_p), ("out_rgba8", C.c_void_p),
+                ("skins", C.c_void_p), ("nskin", C.c_uint32), ("flags", C.c_uint32)]
+
+
 class Context:
     """gbrt_ctx: one CUDA device + stream."""
 
@@ -123,6 +134,14 @@ class Context:
     def sync(self):
         self.check(self.L.gbrt_sync(self.h))
 
+    # -- jobs (asynchronous frames, continuous batching) ----------------------
+    def jobs_configure(self, hbm_budget=0, policy=POLICY_SRPT):
+        self.check(self.L.gbrt_jobs_configure(self.h, hbm_budget, policy))
+
+    def submit(self, scene, ubo, accum, image=True, skins=None):
+        """Queues one frame of `scene` into `accum`; returns a Job."""
+        return Job(self, scene, ubo, accum, image, skins)
+
     def close(self):
         if getattr(self, "h", None):
             self.L.gbrt_ctx_destroy(self.h)
@@ -130,6 +149,46 @@ class Context:
 
     def __del__(self):
         self.close()
+
+
+class Job:
+    """A submitted frame: ``wait()`` returns its info (state, status, queue
+    and end-to-end latency in ms, stats) and fills ``image``."""
+
+    def __init__(self, ctx, scene, ubo, accum, image=True, skins=None):
+        self.ctx = ctx
+        self._ubo = np.asarray(ubo, T.UBO).reshape(())
+        self.image = np.zeros((accum.h_, accum.w, 4), np.uint8) if image else None
+        self._skins = None if skins is None else np.ascontiguousarray(skins, T.SKIN)
+        d = JobDesc(scene.h, self._ubo.ctypes.data, accum.h,
+                    self.image.ctypes.data if image else None,
+                    self._skins.ctypes.data if self._skins is not None else None,
+                    0 if self._skins is None else len(self._skins), 0)
+        jid = u64()
+        ctx.check(ctx.L.gbrt_job_submit(ctx.h, C.byref(d), C.byref(jid)))
+        self.id = jid.value
+        self.info = None
+
+    def _finish(self, rc, info):
+        if rc == E_BUSY:
+            return None
+        self.info = {"state": int(info["state"]), "status": int(info["status"]),
+                     "queue_ms": float(info["queue_ms"]), "latency_ms": float(info["latency_ms"]),
+                     "stats": info["stats"].copy()}
+        self.ctx.check(rc)
+        return self.info
+
+    def poll(self):
+        if self.info is not None:
+            return self.info
+        info = np.zeros((), T.JOB_INFO)
+        return self._finish(self.ctx.L.gbrt_job_poll(self.ctx.h, self.id, _p(info)), info)
+
+    def wait(self, timeout_ms=0xFFFFFFFF):
+        if self.info is not None:
+            return self.info
+        info = np.zeros((), T.JOB_INFO)
+        return self._finish(self.ctx.L.gbrt_job_wait(self.ctx.h, self.id, timeout_ms, _p(info)), info)
 
 
 class Accum:

@@ -68,8 +68,12 @@ STATS = np.dtype([("rays_total", "<u8"), ("rays_camera", "<u8"), ("rays_extensio
 
 SKIN = np.dtype([("joints", "<f4", (256, 16))])
 
+JOB_INFO = np.dtype([("state", "<u4"), ("status", "<i4"), ("queue_ms", "<f8"), ("latency_ms", "<f8"),
+                     ("stats", STATS)])
+
 for _dt, _size in ((VERTEX, 128), (PRIMINFO, 16), (MATERIAL, 256), (LIGHT, 48), (UBO, 324),
-                   (INSTANCE, 64), (GEO_RANGE, 16), (RAY, 32), (HIT, 24), (STATS, 104), (SKIN, 16384)):
+                   (INSTANCE, 64), (GEO_RANGE, 16), (RAY, 32), (HIT, 24), (STATS, 104), (SKIN, 16384),
+                   (JOB_INFO, 128)):
     assert _dt.itemsize == _size, (_dt, _dt.itemsize, _size)
 assert MATERIAL.fields["base_color"][1] == 32
 assert MATERIAL.fields["attenuation_color"][1] == 128

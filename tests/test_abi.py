@@ -4,6 +4,8 @@ the header's static_asserts pin.  No GPU work runs here."""
 import os
 import re
 
+import ctypes as C
+
 import pytest
 
 from rustracer_gb300 import build, gbrt, types as T
@@ -37,6 +39,7 @@ def test_version_string():
 def test_struct_sizes():
     assert T.VERTEX.itemsize == 128 and T.MATERIAL.itemsize == 256 and T.UBO.itemsize == 324
     assert T.LIGHT.itemsize == 48 and T.INSTANCE.itemsize == 64 and T.PRIMINFO.itemsize == 16
+    assert T.JOB_INFO.itemsize == 128 and C.sizeof(gbrt.JobDesc) == 48
 
 
 def test_no_device_is_an_error_not_a_crash():

@@ -1,0 +1,117 @@
+"""Job API (gbrt_job_submit / poll / wait): continuous batching of frames of
+several scenes in shared waves.
+
+The contract: a job's accumulation buffer and image are bit-identical to
+the same frame rendered alone through gbrt_render_ex (wavefront mode),
+whatever other jobs share its waves and however its pixels and samples are
+split across waves.
+"""
+import numpy as np
+import pytest
+
+from rustracer_gb300 import scenes, zoo
+
+pytestmark = pytest.mark.gpu
+
+
+def _solo(ctx, sc, ubo, w, h):
+    from rustracer_gb300 import gbrt
+    acc = gbrt.Accum(ctx, w, h)
+    r = sc.render(ubo, acc, mode=gbrt.MODE_WAVEFRONT)
+    return r["image"], acc.download()
+
+
+def test_single_job_matches_render(gpu_ctx):
+    from rustracer_gb300 import gbrt
+    sd = scenes.cornell()
+    sc = gbrt.Scene(gpu_ctx, sd)
+    ubo = sd.ubo(128, 96, samples=6, bounces=8, exposure=1.0)
+    img, acc_ref = _solo(gpu_ctx, sc, ubo, 128, 96)
+    acc = gbrt.Accum(gpu_ctx, 128, 96)
+    job = gpu_ctx.submit(sc, ubo, acc)
+    info = job.wait()
+    assert info["state"] == gbrt.JOB_DONE and info["status"] == 0
+    assert np.array_equal(job.image.reshape(img.shape), img)
+    assert np.array_equal(acc.download(), acc_ref)
+    st = info["stats"]
+    assert st["rays_camera"] == 128 * 96 * 6 and st["rays_total"] > st["rays_camera"]
+    assert info["latency_ms"] >= info["queue_ms"] >= 0.0
+    # the handle is released once its result has been reported
+    assert gpu_ctx.L.gbrt_job_poll(gpu_ctx.h, job.id, None) == gbrt.E_INVALID
+
+
+def test_mixed_jobs_equal_solo_renders(gpu_ctx):
+    """Twelve jobs on three scenes, sizes from 48x32 to 1280x720 and 1-16
+    spp, submitted at once (many share waves; the large ones span several)."""
+    from rustracer_gb300 import gbrt
+    sds = [scenes.cornell(), scenes.icosphere_scene(subdiv=3), zoo.material_zoo(subdiv=2)]
+    scs = [gbrt.Scene(gpu_ctx, sd) for sd in sds]
+    rng = np.random.default_rng(11)
+    sizes = [(48, 32), (64, 64), (200, 120), (1280, 720), (96, 64), (320, 240)]
+    specs = []
+    for i in range(12):
+        k = i % 3
+        w, h = sizes[rng.integers(len(sizes))]
+        spp = int(rng.choice([1, 2, 4, 16]))
+        ubo = sds[k].ubo(w, h, samples=spp, bounces=int(rng.integers(3, 9)), exposure=1.0, has_sky=(k == 2))
+        specs.append((k, w, h, ubo))
+    solo = [_solo(gpu_ctx, scs[k], ubo, w, h) for k, w, h, ubo in specs]
+    accs = [gbrt.Accum(gpu_ctx, w, h) for _, w, h, _ in specs]
+    jobs = [gpu_ctx.submit(scs[k], ubo, accs[i]) for i, (k, w, h, ubo) in enumerate(specs)]
+    for i, j in enumerate(jobs):
+        info = j.wait()
+        assert info["status"] == 0, i
+        img, acc = solo[i]
+        assert np.array_equal(j.image.reshape(img.shape), img), i
+        assert np.array_equal(accs[i].download(), acc), i
+
+
+def test_policies_agree(gpu_ctx):
+    """Submission-order and shortest-first filling give the same images."""
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=2)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    ubos = [sd.ubo(160, 90, samples=s, bounces=6, exposure=1.0) for s in (8, 1, 3)]
+    out = []
+    for pol in (gbrt.POLICY_FIFO, gbrt.POLICY_SRPT):
+        gpu_ctx.jobs_configure(policy=pol)
+        accs = [gbrt.Accum(gpu_ctx, 160, 90) for _ in ubos]
+        js = [gpu_ctx.submit(sc, u, a) for u, a in zip(ubos, accs)]
+        out.append([(j.wait(), j.image.copy())[1] for j in js])
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+def test_skinned_job_equals_skin_then_render(gpu_ctx):
+    from rustracer_gb300 import gbrt
+    sd = zoo.skinned_tube()
+    ubo = sd.ubo(96, 96, samples=2, bounces=6, exposure=1.0)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    ref = []
+    for t in (0.4, 1.6):
+        sc.skin_and_refit(zoo.bone_matrices(sd.bones, t))
+        ref.append(_solo(gpu_ctx, sc, ubo, 96, 96))
+    accs = [gbrt.Accum(gpu_ctx, 96, 96) for _ in range(2)]
+    jobs = [gpu_ctx.submit(sc, ubo, accs[i], skins=zoo.bone_matrices(sd.bones, t)) for i, t in enumerate((0.4, 1.6))]
+    for i, j in enumerate(jobs):
+        assert j.wait()["status"] == 0
+        assert np.array_equal(j.image.reshape(ref[i][0].shape), ref[i][0]), i
+        assert np.array_equal(accs[i].download(), ref[i][1]), i
+
+
+def test_busy_while_jobs_outstanding(gpu_ctx):
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=4)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    big = sd.ubo(1280, 720, samples=32, bounces=8, exposure=1.0)
+    acc = gbrt.Accum(gpu_ctx, 1280, 720)
+    job = gpu_ctx.submit(sc, big, acc, image=False)
+    with pytest.raises(gbrt.GbrtError) as e:
+        sc.render(sd.ubo(16, 16, samples=1), gbrt.Accum(gpu_ctx, 16, 16))
+    assert e.value.code == gbrt.E_BUSY
+    with pytest.raises(gbrt.GbrtError) as e:
+        acc.reset()
+    assert e.value.code == gbrt.E_BUSY
+    assert job.poll() is None or job.info["state"] == gbrt.JOB_DONE
+    assert job.wait()["status"] == 0
+    sc.render(sd.ubo(16, 16, samples=1), gbrt.Accum(gpu_ctx, 16, 16))  # usable again
