@@ -287,6 +287,173 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def oracle_bytes_per_ray(sd, depth, w=96, h=54):
+    """B_ray of one scene: 48 + 64 N_node + 36 N_tri from the oracle's BVH2
+    on a small camera-driven sample (w x h at 1 spp, same depth)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    st = O.OracleScene(sd).render(sd.ubo(w, h, samples=1, bounces=depth, exposure=1.0), w, h, out=False)["stats"]
+    rays = int(st["rays_camera"] + st["rays_extension"] + st["rays_shadow"])
+    return 48.0 + (64.0 * int(st["node_visits"]) + 36.0 * int(st["tri_tests"])) / max(rays, 1)
+
+
+def job_rays(info):
+    st = info["stats"]
+    return int(st["rays_total"]), int(st["hits_shaded"])
+
+
+def run_batched(args):
+    """32 seeded instanced scenes (alpha-tested, transmissive materials),
+    each with its own resolution and spp, rendered as one batch of jobs that
+    share waves (continuous batching); a step = the 32 frames.  Also times
+    the same frames rendered one after another through gbrt_render_ex."""
+    from rustracer_gb300 import build, gbrt, workloads as WL
+    build.build()
+    depth = DEPTH
+    specs = [WL.batched_scene(i) for i in range(32)]
+    ctx = gbrt.Context(0)
+    scs = [gbrt.Scene(ctx, sd) for sd, _, _, _ in specs]
+    accs = [gbrt.Accum(ctx, w, h) for _, w, h, _ in specs]
+    ubos = [sd.ubo(w, h, samples=spp, bounces=depth, exposure=1.0) for sd, w, h, spp in specs]
+    pinned = [np.zeros((h, w, 4), np.uint8) for _, w, h, _ in specs]
+
+    def batch():
+        jobs = [ctx.submit(sc, u, a) for sc, u, a in zip(scs, ubos, accs)]
+        infos = [j.wait() for j in jobs]
+        for j in jobs:
+            assert j.info["status"] == 0
+        return infos
+
+    def sequential():
+        rays = 0
+        for sc, u, a, img in zip(scs, ubos, accs, pinned):
+            st = np.zeros((), gbrt.T.STATS)
+            ctx.check(ctx.L.gbrt_render_ex(sc.h, gbrt._p(np.asarray(u).reshape(())), a.h, gbrt._p(img),
+                                           gbrt._p(st), C.byref(gbrt.RenderOpts(MODES["wavefront"], 0, None, None))))
+            rays += int(st["rays_total"])
+        return rays
+
+    for _ in range(args.warmup):
+        batch()
+    rays = shaded = 0
+    per_scene = [0] * 32
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            infos = batch()
+            for i, inf in enumerate(infos):
+                r, sh = job_rays(inf)
+                rays += r
+                shaded += sh
+                per_scene[i] += r
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    t1 = time.perf_counter()
+    seq_rays = sum(sequential() for _ in range(args.steps))
+    seq_wall = time.perf_counter() - t1
+    brays = [oracle_bytes_per_ray(sd, depth) for sd, _, _, _ in specs]
+    alg_bytes = sum(per_scene[i] * brays[i] for i in range(32)) + shaded * B_SHADE
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / wall / 1e9
+    value = rays / wall / 1e6
+    px = sum(w * h * spp for _, w, h, spp in specs)
+    line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (32 seeded scenes of instanced tori, 1k-2M triangles per mesh)",
+            "config": {"workload": "batched32_instanced_alpha_transmissive", "scenes": 32,
+                       "triangles_unique": int(sum(sd.num_triangles for sd, _, _, _ in specs)),
+                       "instances": int(sum(len(sd.instances) for sd, _, _, _ in specs)),
+                       "paths_per_step": int(px), "depth": depth,
+                       "resolutions": "{256^2, 512^2, 1280x720, 1920x1080}", "spp": "{1, 4, 16, 64}",
+                       "l2": "inputs (1.2 GB of vertices) larger than L2", "timing": "host wall clock, submit to last image on host"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind, "kernel": "whole batch (algorithmic bytes)",
+                         "bytes_per_ray_by_scene": [round(b, 1) for b in brays]},
+            "sequential": {"value": seq_rays / seq_wall / 1e6, "unit": "Mrays/s",
+                           "how": "the same 32 frames one after another through gbrt_render_ex"},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * 324,
+                    "d2h_bytes_per_step": int(sum(w * h * 4 for _, w, h, _ in specs))},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    """Serving loop: seeded Poisson arrivals (rate --rate jobs/s, --jobs of
+    them) over a pool of 8 scenes (10k-5M triangles, one a 64-bone skinned
+    tube re-skinned and rebuilt for every job on it); resolution log-uniform
+    256^2..1920x1080, spp log-uniform 1..256.  Latency = submit -> image on
+    the host.  Reports p50/p99 latency, Mrays/s over the run, HBM fraction."""
+    import threading as th
+    from rustracer_gb300 import build, gbrt, workloads as WL, zoo
+    build.build()
+    depth = DEPTH
+    pool = WL.serving_pool()
+    trace = WL.serving_trace(seed=0, n=args.jobs, rate=args.rate)
+    ctx = gbrt.Context(0)
+    scs = [gbrt.Scene(ctx, sd) for sd in pool]
+    bones = pool[7].bones
+    accs = [gbrt.Accum(ctx, j["width"], j["height"]) for j in trace]
+    ubos = [pool[j["scene"]].ubo(j["width"], j["height"], samples=j["spp"], bounces=depth, exposure=1.0)
+            for j in trace]
+    skins = [zoo.bone_matrices(bones, j["anim_time"]) if j["anim_time"] is not None else None for j in trace]
+    # warm-up: one small job per scene
+    warm = [gbrt.Accum(ctx, 64, 64) for _ in scs]
+    for _ in range(max(1, args.warmup)):
+        ws = [ctx.submit(sc, pool[k].ubo(64, 64, samples=1, bounces=depth, exposure=1.0), warm[k],
+                         skins=zoo.bone_matrices(bones, 0.0) if k == 7 else None) for k, sc in enumerate(scs)]
+        for w in ws:
+            w.wait()
+    jobs = [None] * len(trace)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, j in enumerate(trace):
+                dt = t0 + j["arrival"] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                jobs[i] = ctx.submit(scs[j["scene"]], ubos[i], accs[i], skins=skins[i])
+
+        thr = th.Thread(target=submitter)
+        thr.start()
+        thr.join()
+        infos = [j.wait() for j in jobs]
+        t_end = time.perf_counter()
+    clocks = clk.summary()
+    lat = np.array([inf["latency_ms"] for inf in infos])
+    rays = np.array([job_rays(inf)[0] for inf in infos], np.float64)
+    shaded = np.array([job_rays(inf)[1] for inf in infos], np.float64)
+    assert all(inf["status"] == 0 for inf in infos)
+    makespan = t_end - t0
+    brays = [oracle_bytes_per_ray(sd, depth) for sd in pool]
+    alg = float(sum(rays[i] * brays[trace[i]["scene"]] for i in range(len(trace))) + shaded.sum() * B_SHADE)
+    peak, peak_kind = measured_peaks()
+    paths = np.array([j["width"] * j["height"] * j["spp"] for j in trace], np.float64)
+    value = rays.sum() / makespan / 1e6
+    line = {"metric": "p99 job latency", "value": float(np.percentile(lat, 99)), "unit": "ms", "n_gpus": 1,
+            "steps": 1, "warmup": args.warmup, "ms_per_step": makespan * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded job trace over 8 seeded scenes)",
+            "config": {"workload": f"serving_poisson{args.rate:g}_jobs{args.jobs}", "jobs": args.jobs,
+                       "rate_per_s": args.rate, "scenes": [sd.name for sd in pool],
+                       "triangles": [int(sd.num_triangles) for sd in pool], "depth": depth,
+                       "paths_total": int(paths.sum()), "arrival_span_s": trace[-1]["arrival"],
+                       "policy": "shortest remaining paths first", "skinned_scene": "64-bone tube, skinned + rebuilt per job"},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_queue_ms": float(np.mean([inf["queue_ms"] for inf in infos])),
+            "throughput": {"value": value, "unit": "Mrays/s", "makespan_s": makespan,
+                           "offered_load": float(makespan / max(trace[-1]["arrival"], 1e-9))},
+            "roofline": {"bound": "hbm", "achieved": alg / makespan / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / makespan / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "whole run (algorithmic bytes)",
+                         "bytes_per_ray_by_scene": [round(b, 1) for b in brays]},
+            "e2e": {"value": float(np.percentile(lat, 99)), "unit": "ms", "h2d_bytes_per_step": int(324 * len(trace)),
+                    "d2h_bytes_per_step": int(sum(j["width"] * j["height"] * 4 for j in trace))},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -326,6 +493,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
     ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")
+    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched", "serving"],
+                    help="icosphere: the headline frame; batched: 32 scenes as one batch of jobs; "
+                         "serving: Poisson job arrivals with p50/p99 latency")
+    ap.add_argument("--jobs", type=int, default=200, help="serving: jobs in the trace")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     args = ap.parse_args()
     global W, H, SPP, WORKLOAD
     if args.res:
@@ -335,6 +507,10 @@ def main():
     WORKLOAD = f"icosphere{SUBDIV}_cornell_{W}x{H}_{SPP}spp_depth{DEPTH}"
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_gpu(args)
 
