@@ -137,6 +137,8 @@ void refresh_view(gbrt_scene* s) {
     v.sky_size = s->sky_size;
     v.cw_nodes = s->cw_count ? s->cw_nodes.as<CwNode>() : nullptr;
     v.cw_tris = s->cw_count ? s->cw_tris.as<TriRec>() : nullptr;
+    v.blas_cw_nodes = s->blas_cw_nodes.p ? s->blas_cw_nodes.as<CwNode>() : nullptr;
+    v.blas_cw_tris = s->blas_cw_nodes.p ? s->blas_cw_tris.as<TriRec>() : nullptr;
 }
 
 // Builds the merged world BVH, the BLASes of transformed instances and the
@@ -233,6 +235,16 @@ int build_all(gbrt_scene* s) {
     if (!tlas_ids.empty()) {
         std::vector<float4> blo(s->ngeo), bhi(s->ngeo);
         std::vector<int32_t> broot(s->ngeo, 0);
+        // 8-wide copies of the BLASes: pools with one slot per triangle
+        std::vector<uint32_t> cw_node0(s->ngeo, 0), cw_tri0(s->ngeo, 0);
+        size_t cw_slots = 0;
+        for (uint32_t g = 0; g < s->ngeo; ++g) {
+            if (!blas_needed[g]) continue;
+            cw_node0[g] = cw_tri0[g] = (uint32_t)cw_slots;
+            cw_slots += s->ranges[g].i_len / 3;
+        }
+        CU(c, s->blas_cw_nodes.alloc(std::max<size_t>(1, cw_slots) * sizeof(CwNode)), "cudaMalloc(wide BLAS nodes)");
+        CU(c, s->blas_cw_tris.alloc(std::max<size_t>(1, cw_slots) * sizeof(TriRec)), "cudaMalloc(wide BLAS tris)");
         DevBuf bitems;
         for (uint32_t g = 0; g < s->ngeo; ++g) {
             if (!blas_needed[g]) continue;
@@ -248,12 +260,20 @@ int build_all(gbrt_scene* s) {
             broot[g] = r.root;
             blo[g] = r.lo;
             bhi[g] = r.hi;
+            uint32_t used = 0;
+            CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                       s->prims.as<gbrt_priminfo>(), bitems.as<uint4>(), ntri,
+                                       s->blas_cw_nodes.as<CwNode>() + cw_node0[g],
+                                       s->blas_cw_tris.as<TriRec>() + cw_tri0[g], &used, st),
+               "build wide BLAS");
         }
         const uint32_t nt = (uint32_t)tlas_ids.size();
         std::vector<float4> ilo(nt), ihi(nt);
         for (uint32_t k = 0; k < nt; ++k) {
             DevInstance& d = hinst[tlas_ids[k]];
             d.blas_root = broot[d.blas_geo];
+            d.cw_node0 = cw_node0[d.blas_geo];
+            d.cw_tri0 = cw_tri0[d.blas_geo];
             d.has_blas = 1;
             ilo[k] = blo[d.blas_geo];
             ihi[k] = bhi[d.blas_geo];
@@ -278,6 +298,8 @@ int build_all(gbrt_scene* s) {
         v.tlas_hi = r.hi;
         CU(c, cudaStreamSynchronize(st), "sync after TLAS build");
     } else {
+        s->blas_cw_nodes.release();
+        s->blas_cw_tris.release();
         CU(c, upload(s->inst, hinst.data(), std::max<size_t>(hinst.size(), 0), st), "upload(instances)");
         if (hinst.empty()) CU(c, s->inst.alloc(sizeof(DevInstance)), "cudaMalloc");
         CU(c, cudaStreamSynchronize(st), "sync after build");

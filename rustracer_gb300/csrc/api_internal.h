@@ -82,6 +82,7 @@ struct gbrt_scene {
     // acceleration structures
     gbrt_host::DevBuf nodes, tris, inst, items;
     gbrt_host::DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
+    gbrt_host::DevBuf blas_cw_nodes, blas_cw_tris;  // 8-wide BLASes of transformed instances
     uint32_t cw_count = 0;
     bool built = false;
     std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene

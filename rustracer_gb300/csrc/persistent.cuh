@@ -171,77 +171,9 @@ GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32
 
 namespace gbrt {
 
-constexpr int kCwStack = 32;
-
-// Byte k of an 8-byte group (lo word = bytes 0..3) as the float
-// 1 + q * 2^-15, in one byte permute: result bytes (from low) = 0x00, q, 0x80,
-// 0x3F, i.e. 0x3F80qq00.
-GB_D float cw_q(uint32_t lo, uint32_t hi, int k) {
-    const uint32_t w = k < 4 ? lo : hi;
-    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)(k & 3) << 4)));
-}
-
-// Intersects the 8 children of wide node `node`: returns the hit mask (bits
-// 24 + (slot ^ oct) for inner children, triangle bits 0..23 for leaves) and
-// the node's child base, triangle base and inner-slot mask.
-GB_D uint32_t cw_intersect(const DevScene& s, uint32_t node, const TRay& r, uint32_t oct, float tmin, float tmax,
-                           uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
-    const uint4* np = reinterpret_cast<const uint4*>(s.cw_nodes + node);
-    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-    child_base = w1.x;
-    tri_base = w1.y;
-    imask = w0.w >> 24;
-    // per axis: t = o + q * s = fma(1 + q 2^-15, 2^15 s, o - 2^15 s).  An axis the
-    // ray is parallel to (d = 0) gives (-inf, +inf) and the origin must lie
-    // inside that child's slab instead.
-    const float scx = __uint_as_float((w0.w & 0xFFu) << 23);
-    const float scy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23);
-    const float scz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23);
-    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-    const bool zx = r.d.x == 0.0f, zy = r.d.y == 0.0f, zz = r.d.z == 0.0f;
-    const float Sx = zx ? 0.0f : 32768.0f * (scx * r.inv.x);
-    const float Sy = zy ? 0.0f : 32768.0f * (scy * r.inv.y);
-    const float Sz = zz ? 0.0f : 32768.0f * (scz * r.inv.z);
-    const float Ox = (px - r.o.x) * r.inv.x - Sx, Oy = (py - r.o.y) * r.inv.y - Sy, Oz = (pz - r.o.z) * r.inv.z - Sz;
-    const float Oxn = zx ? -INFINITY : Ox, Oxf = zx ? INFINITY : Ox;
-    const float Oyn = zy ? -INFINITY : Oy, Oyf = zy ? INFINITY : Oy;
-    const float Ozn = zz ? -INFINITY : Oz, Ozf = zz ? INFINITY : Oz;
-    const bool parallel = zx || zy || zz;
-    // near / far planes per axis by direction sign
-    const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
-    const uint32_t lnx0 = nx ? w3.z : w2.x, lnx1 = nx ? w3.w : w2.y, lfx0 = nx ? w2.x : w3.z, lfx1 = nx ? w2.y : w3.w;
-    const uint32_t lny0 = ny ? w4.x : w2.z, lny1 = ny ? w4.y : w2.w, lfy0 = ny ? w2.z : w4.x, lfy1 = ny ? w2.w : w4.y;
-    const uint32_t lnz0 = nz ? w4.z : w3.x, lnz1 = nz ? w4.w : w3.y, lfz0 = nz ? w3.x : w4.z, lfz1 = nz ? w3.y : w4.w;
-    uint32_t hits = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t meta = ((k < 4 ? w1.z : w1.w) >> (8 * (k & 3))) & 0xFFu;
-        const float tnx = fmaf(cw_q(lnx0, lnx1, k), Sx, Oxn), tfx = fmaf(cw_q(lfx0, lfx1, k), Sx, Oxf);
-        const float tny = fmaf(cw_q(lny0, lny1, k), Sy, Oyn), tfy = fmaf(cw_q(lfy0, lfy1, k), Sy, Oyf);
-        const float tnz = fmaf(cw_q(lnz0, lnz1, k), Sz, Ozn), tfz = fmaf(cw_q(lfz0, lfz1, k), Sz, Ozf);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-        bool inside = true;
-        if (parallel) {  // decoded slab of each parallel axis must contain the origin
-            auto in = [&](bool z, uint32_t lo0, uint32_t lo1, uint32_t hi0, uint32_t hi1, float p, float sc, float o) {
-                if (!z) return true;
-                const float ql = (cw_q(lo0, lo1, k) - 1.0f) * 32768.0f, qh = (cw_q(hi0, hi1, k) - 1.0f) * 32768.0f;
-                return o >= p + ql * sc && o <= p + qh * sc;
-            };
-            inside = in(zx, w2.x, w2.y, w3.z, w3.w, px, scx, r.o.x) && in(zy, w2.z, w2.w, w4.x, w4.y, py, scy, r.o.y) &&
-                     in(zz, w3.x, w3.y, w4.z, w4.w, pz, scz, r.o.z);
-        }
-        // empty slots (meta 0) contribute no bit
-        const uint32_t low = meta & 0x1Fu;
-        const uint32_t bits = low >= 24u ? (1u << (24u + ((uint32_t)k ^ oct))) : ((meta >> 5) << low);
-        hits |= (tn <= tf && inside) ? bits : 0u;
-    }
-    return hits;
-}
-
 // Persistent-lane traversal of the 8-wide world BVH; same interface and
 // refill policy as persistent_trace.
-template <bool kAny, class Loader, class Finisher>
+template <bool kAny, bool kTlas, class Loader, class Finisher>
 GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts,
                               Loader&& load, Finisher&& finish) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -309,7 +241,7 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
                 else ts.status |= GBRT_STATUS_STACK_OVERFLOW;
             }
             uint32_t cb, tb, im;
-            const uint32_t hm = cw_intersect(s, child, r, oct, tmin, best.t, cb, tb, im);
+            const uint32_t hm = cw_intersect(s.cw_nodes, child, r, oct, tmin, best.t, cb, tb, im);
             ts.nodes++;
             ng = make_uint2(cb, (hm & 0xFF000000u) | im);
             uint32_t tri_bits = hm & 0x00FFFFFFu;
@@ -340,20 +272,36 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
             }
         }
         if (done) {
-            if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu))
-                trace_tlas<kAny>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);
+            if constexpr (kTlas) {
+                if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu))
+                    trace_tlas<kAny, true>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);
+            }
             finish(q, best.inst != 0xFFFFFFFFu, best);
             has = false;
         }
     }
 }
 
-// World traversal in the layout the scene carries (8-wide when built).
-template <bool kAny, bool kWide, class Loader, class Finisher>
+// Traversal forms of a world query (chosen per launch by trace_mode):
+//   kTraceBinary  binary world BVH, binary BLASes (scenes without 8-wide nodes)
+//   kTraceWide    8-wide world BVH, no transformed instances
+//   kTraceWideTlas 8-wide world BVH, then the TLAS with 8-wide BLASes
+// Keeping the TLAS code out of the common form keeps its registers free.
+constexpr int kTraceBinary = 0, kTraceWide = 1, kTraceWideTlas = 2;
+
+template <bool kAny, int kMode, class Loader, class Finisher>
 GB_D void world_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts, Loader&& load,
                       Finisher&& finish) {
-    if (kWide) persistent_trace_cw<kAny>(s, n, work, flags, ts, load, finish);
-    else persistent_trace<kAny>(s, n, work, flags, ts, load, finish);
+    if constexpr (kMode == kTraceBinary) persistent_trace<kAny>(s, n, work, flags, ts, load, finish);
+    else persistent_trace_cw<kAny, kMode == kTraceWideTlas>(s, n, work, flags, ts, load, finish);
+}
+
+// The form a scene needs: binary when it has a world BVH without its
+// 8-wide copy (after gbrt_scene_rebuild_noalloc), else 8-wide, with the TLAS
+// when it has transformed instances.
+inline int trace_mode(const DevScene& s) {
+    if (s.has_world && !s.cw_nodes) return kTraceBinary;
+    return s.has_tlas ? kTraceWideTlas : kTraceWide;
 }
 
 }  // namespace gbrt

@@ -6,12 +6,12 @@ namespace gbrt {
 
 // traceRayEXT queries (gbrt_trace_rays) through the persistent traversal of
 // the world BVH in the layout the scene carries.
-template <bool kAny, bool kWide>
+template <bool kAny, int kMode>
 __global__ void __launch_bounds__(128) trace_rays_persistent(DevScene s, const gbrt_ray* rays, uint32_t n,
                                                              uint32_t flags, gbrt_hit* hits, uint32_t* work,
                                                              DeviceCounters* cnt) {
     TraceStats ts{0, 0, 0};
-    world_trace<kAny, kWide>(
+    world_trace<kAny, kMode>(
         s, n, work, flags, ts,
         [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
             const gbrt_ray r = rays[q];
@@ -54,7 +54,7 @@ cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays
     if (dev != dev_cached) {
         int sms = 0, per = 0;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_rays_persistent<false, true>, 128, 0)) !=
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_rays_persistent<false, kTraceWideTlas>, 128, 0)) !=
             cudaSuccess)
             return e;
         resident = sms * (per > 0 ? per : 1);
@@ -64,12 +64,14 @@ cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays
     const uint32_t need = (n + 127) / 128;
     const uint32_t grid = need < (uint32_t)resident ? need : (uint32_t)resident;
     const bool any = flags & GBRT_RAY_TERMINATE_ON_FIRST;
-    if (s.cw_nodes) {
-        if (any) trace_rays_persistent<true, true><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
-        else trace_rays_persistent<false, true><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+    // ray queries use the 8-wide form with the TLAS (it skips the TLAS of
+    // scenes without one), or the binary form where the scene needs it
+    if (trace_mode(s) != kTraceBinary) {
+        if (any) trace_rays_persistent<true, kTraceWideTlas><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+        else trace_rays_persistent<false, kTraceWideTlas><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
     } else {
-        if (any) trace_rays_persistent<true, false><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
-        else trace_rays_persistent<false, false><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+        if (any) trace_rays_persistent<true, kTraceBinary><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
+        else trace_rays_persistent<false, kTraceBinary><<<grid, 128, 0, st>>>(s, rays, n, flags, hits, work, cnt);
     }
     return cudaGetLastError();
 }

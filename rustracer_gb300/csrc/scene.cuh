@@ -68,7 +68,8 @@ struct DevInstance {
     int32_t blas_root; // root of that BLAS in the pool (node index or leaf code)
     uint32_t has_blas; // 0 when the geometry has no triangles
     uint32_t identity; // 1 = merged into the world BVH
-    uint32_t _pad[2];
+    uint32_t cw_node0; // its 8-wide BLAS: first node and first triangle slot in the BLAS pools
+    uint32_t cw_tri0;
 };
 
 struct DevTexture {
@@ -85,6 +86,8 @@ struct DevScene {
     int32_t tlas_root;    // valid when has_tlas
     const CwNode* cw_nodes;  // 8-wide world BVH (root = node 0), null if not built
     const TriRec* cw_tris;   //   its triangles, in node-leaf order
+    const CwNode* blas_cw_nodes;  // 8-wide BLASes of transformed instances (null: binary BLASes)
+    const TriRec* blas_cw_tris;
     uint32_t has_world;   // some identity instance exists
     uint32_t has_tlas;    // some transformed instance exists
     float4 world_lo, world_hi;  // bounds of the world BVH root

@@ -12,6 +12,7 @@
 #include <float.h>
 #include "shade.cuh"
 
+
 namespace gbrt {
 
 constexpr int kStack = 64;
@@ -212,11 +213,139 @@ GB_D bool traverse_bvh(const DevScene& s, int root, const TRay& r, float tmin, H
     }
 }
 
+constexpr int kCwStack = 32;
+
+// Byte k of an 8-byte group (lo word = bytes 0..3) as the float
+// 1 + q * 2^-15, in one byte permute: result bytes (from low) = 0x00, q, 0x80,
+// 0x3F, i.e. 0x3F80qq00.
+GB_D float cw_q(uint32_t lo, uint32_t hi, int k) {
+    const uint32_t w = k < 4 ? lo : hi;
+    return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)(k & 3) << 4)));
+}
+
+// Intersects the 8 children of wide node `node`: returns the hit mask (bits
+// 24 + (slot ^ oct) for inner children, triangle bits 0..23 for leaves) and
+// the node's child base, triangle base and inner-slot mask.
+GB_D uint32_t cw_intersect(const CwNode* nodes, uint32_t node, const TRay& r, uint32_t oct, float tmin, float tmax,
+                           uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
+    const uint4* np = reinterpret_cast<const uint4*>(nodes + node);
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    child_base = w1.x;
+    tri_base = w1.y;
+    imask = w0.w >> 24;
+    // per axis: t = o + q * s = fma(1 + q 2^-15, 2^15 s, o - 2^15 s).  An axis the
+    // ray is parallel to (d = 0) gives (-inf, +inf) and the origin must lie
+    // inside that child's slab instead.
+    const float scx = __uint_as_float((w0.w & 0xFFu) << 23);
+    const float scy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23);
+    const float scz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23);
+    const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+    const bool zx = r.d.x == 0.0f, zy = r.d.y == 0.0f, zz = r.d.z == 0.0f;
+    const float Sx = zx ? 0.0f : 32768.0f * (scx * r.inv.x);
+    const float Sy = zy ? 0.0f : 32768.0f * (scy * r.inv.y);
+    const float Sz = zz ? 0.0f : 32768.0f * (scz * r.inv.z);
+    const float Ox = (px - r.o.x) * r.inv.x - Sx, Oy = (py - r.o.y) * r.inv.y - Sy, Oz = (pz - r.o.z) * r.inv.z - Sz;
+    const float Oxn = zx ? -INFINITY : Ox, Oxf = zx ? INFINITY : Ox;
+    const float Oyn = zy ? -INFINITY : Oy, Oyf = zy ? INFINITY : Oy;
+    const float Ozn = zz ? -INFINITY : Oz, Ozf = zz ? INFINITY : Oz;
+    const bool parallel = zx || zy || zz;
+    // near / far planes per axis by direction sign
+    const bool nx = r.inv.x < 0.0f, ny = r.inv.y < 0.0f, nz = r.inv.z < 0.0f;
+    const uint32_t lnx0 = nx ? w3.z : w2.x, lnx1 = nx ? w3.w : w2.y, lfx0 = nx ? w2.x : w3.z, lfx1 = nx ? w2.y : w3.w;
+    const uint32_t lny0 = ny ? w4.x : w2.z, lny1 = ny ? w4.y : w2.w, lfy0 = ny ? w2.z : w4.x, lfy1 = ny ? w2.w : w4.y;
+    const uint32_t lnz0 = nz ? w4.z : w3.x, lnz1 = nz ? w4.w : w3.y, lfz0 = nz ? w3.x : w4.z, lfz1 = nz ? w3.y : w4.w;
+    uint32_t hits = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t meta = ((k < 4 ? w1.z : w1.w) >> (8 * (k & 3))) & 0xFFu;
+        const float tnx = fmaf(cw_q(lnx0, lnx1, k), Sx, Oxn), tfx = fmaf(cw_q(lfx0, lfx1, k), Sx, Oxf);
+        const float tny = fmaf(cw_q(lny0, lny1, k), Sy, Oyn), tfy = fmaf(cw_q(lfy0, lfy1, k), Sy, Oyf);
+        const float tnz = fmaf(cw_q(lnz0, lnz1, k), Sz, Ozn), tfz = fmaf(cw_q(lfz0, lfz1, k), Sz, Ozf);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        bool inside = true;
+        if (parallel) {  // decoded slab of each parallel axis must contain the origin
+            auto in = [&](bool z, uint32_t lo0, uint32_t lo1, uint32_t hi0, uint32_t hi1, float p, float sc, float o) {
+                if (!z) return true;
+                const float ql = (cw_q(lo0, lo1, k) - 1.0f) * 32768.0f, qh = (cw_q(hi0, hi1, k) - 1.0f) * 32768.0f;
+                return o >= p + ql * sc && o <= p + qh * sc;
+            };
+            inside = in(zx, w2.x, w2.y, w3.z, w3.w, px, scx, r.o.x) && in(zy, w2.z, w2.w, w4.x, w4.y, py, scy, r.o.y) &&
+                     in(zz, w3.x, w3.y, w4.z, w4.w, pz, scz, r.o.z);
+        }
+        // empty slots (meta 0) contribute no bit
+        const uint32_t low = meta & 0x1Fu;
+        const uint32_t bits = low >= 24u ? (1u << (24u + ((uint32_t)k ^ oct))) : ((meta >> 5) << low);
+        hits |= (tn <= tf && inside) ? bits : 0u;
+    }
+    return hits;
+}
+
+// Stack traversal of one 8-wide BLAS (nodes / tris: its own arrays, root at
+// node 0) for a ray already in object space; hits report instance `inst`.
+// Returns true when kTerminateOnFirst and a hit was accepted.
+//
+// Out of line on purpose: inlined next to the world traversal's own 8-wide
+// loop, the second copy of the node decode made the TLAS kernels 1.8x slower
+// (32 instanced scenes: 232 vs 425 Mrays/s on GB300), while the call costs
+// little -- it runs once per instance a ray reaches.
+template <bool kTerminateOnFirst>
+__device__ __noinline__ bool traverse_cw(const DevScene& s, const CwNode* nodes, const TriRec* tris, const TRay& r, float tmin,
+                      Hit& best, bool test_alpha, const AnyCtx& ctx, TraceStats& ts, uint32_t inst) {
+    const uint32_t oct = (r.d.x < 0.0f ? 1u : 0u) | (r.d.y < 0.0f ? 2u : 0u) | (r.d.z < 0.0f ? 4u : 0u);
+    uint2 stack[kCwStack];
+    int sp = 0;
+    uint2 ng = make_uint2(0u, (1u << (24u + oct)) | 1u);  // virtual parent of the root
+    uint32_t iter = 0;
+    for (;;) {
+        while (!(ng.y & 0xFF000000u) && sp > 0) ng = stack[--sp];
+        if (!(ng.y & 0xFF000000u)) return false;
+        if (++iter > kMaxIter) {
+            ts.status |= GBRT_STATUS_ITER_LIMIT;
+            return false;
+        }
+        const uint32_t bit = __ffs(ng.y & 0xFF000000u) - 1u;
+        ng.y &= ~(1u << bit);
+        const uint32_t slot = (bit - 24u) ^ oct;
+        const uint32_t child = ng.x + __popc((ng.y & 0xFFu) & ((1u << slot) - 1u));
+        if (ng.y & 0xFF000000u) {
+            if (sp < kCwStack) stack[sp++] = ng;
+            else ts.status |= GBRT_STATUS_STACK_OVERFLOW;
+        }
+        uint32_t cb, tb, im;
+        const uint32_t hm = cw_intersect(nodes, child, r, oct, tmin, best.t, cb, tb, im);
+        ts.nodes++;
+        ng = make_uint2(cb, (hm & 0xFF000000u) | im);
+        uint32_t tri_bits = hm & 0x00FFFFFFu;
+        while (tri_bits) {
+            const uint32_t tbit = __ffs(tri_bits) - 1u;
+            tri_bits &= tri_bits - 1u;
+            const TriRec* tr = tris + tb + tbit;
+            const float4 pa = __ldg(&tr->a), pb = __ldg(&tr->b), pc = __ldg(&tr->c);
+            ts.tris++;
+            float t, u, v;
+            if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+            const uint32_t prim = __float_as_uint(pb.w);
+            const uint32_t gw = __float_as_uint(pc.w);
+            if (!closer(t, inst, prim, best)) continue;
+            if (test_alpha && !(gw >> 31) && anyhit_ignore(s, s.inst[inst].custom, prim, inst, u, v, ctx)) continue;
+            best.t = t;
+            best.u = u;
+            best.v = v;
+            best.inst = inst;
+            best.prim = prim;
+            best.bgeo = gw & 0x7FFFFFFFu;
+            if (kTerminateOnFirst) return true;
+        }
+    }
+}
+
 // The TLAS part of a query: transformed instances, each BLAS traversed in
 // object space with the world-to-object transform applied unfused (like the
 // oracle), updating `best`.  Returns true when a terminate-on-first query
-// found a hit.
-template <bool kTerminateOnFirst>
+// found a hit.  kCwBlas: the BLASes are traversed in their 8-wide form
+// (built for every BLAS), else in the binary form.
+template <bool kTerminateOnFirst, bool kCwBlas = false>
 GB_D bool trace_tlas(const DevScene& s, const TRay& r, float3 o, float3 d, float tmin, Hit& best, bool test_alpha,
                      const AnyCtx& ctx, TraceStats& st) {
     {
@@ -253,9 +382,16 @@ GB_D bool trace_tlas(const DevScene& s, const TRay& r, float3 o, float3 d, float
                         if ((in.mask & 0xFFu) == 0u || !in.has_blas) continue;
                         TRay orr;
                         setup_ray(orr, xform34_rn(in.inv, o, 1.0f), xform34_rn(in.inv, d, 0.0f));
-                        if (traverse_bvh<kTerminateOnFirst>(s, in.blas_root, orr, tmin, best, test_alpha, ctx, st,
-                                                            (int)ii))
-                            return true;
+                        if constexpr (kCwBlas) {
+                            if (traverse_cw<kTerminateOnFirst>(s, s.blas_cw_nodes + in.cw_node0,
+                                                               s.blas_cw_tris + in.cw_tri0, orr, tmin, best,
+                                                               test_alpha, ctx, st, ii))
+                                return true;
+                        } else {
+                            if (traverse_bvh<kTerminateOnFirst>(s, in.blas_root, orr, tmin, best, test_alpha, ctx,
+                                                                st, (int)ii))
+                                return true;
+                        }
                     }
                 }
                 if (sp == 0) break;

@@ -50,14 +50,14 @@ struct MultiWave {
 }  // namespace
 
 __global__ void __launch_bounds__(128) wfm_camera(WfState st) { camera_body(MultiWave{}, st); }
-template <bool kWide>
-__global__ void __launch_bounds__(128, GBRT_TRACE_MINB) wfm_extend(WfState st, uint32_t b) {
-    extend_body<kWide>(MultiWave{}, st, b);
+template <int kMode>
+__global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_extend(WfState st, uint32_t b) {
+    extend_body<kMode>(MultiWave{}, st, b);
 }
 __global__ void __launch_bounds__(128) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
-template <bool kWide>
-__global__ void __launch_bounds__(128, GBRT_TRACE_MINB) wfm_shadow(WfState st, uint32_t b) {
-    shadow_body<kWide>(MultiWave{}, st, b);
+template <int kMode>
+__global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_shadow(WfState st, uint32_t b) {
+    shadow_body<kMode>(MultiWave{}, st, b);
 }
 __global__ void __launch_bounds__(128) wfm_finish(WfState st) { finish_body(MultiWave{}, st); }
 
@@ -80,9 +80,9 @@ cudaError_t grids(Grid& g) {
     if (g.dev == dev) return cudaSuccess;
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wfm_extend<true>, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wfm_extend<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wfm_shade, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wfm_shadow<true>, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wfm_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
     g.shadow = sms * (bh > 0 ? bh : 1);
@@ -155,8 +155,12 @@ cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, 
     ring.next = (ring.next + 1) % WaveRing::kSlots;
     if ((e = cudaMemsetAsync(st.counts, 0, (size_t)w.njobs * kWfCounters * sizeof(uint32_t), stream)) != cudaSuccess)
         return e;
-    bool wide = true;  // the 8-wide traversal when every job's scene carries it
-    for (uint32_t j = 0; j < w.njobs; ++j) wide = wide && w.jobs[j].s.cw_nodes;
+    int mode = kTraceWide;  // the most general form any job's scene needs
+    for (uint32_t j = 0; j < w.njobs; ++j) {
+        const int m = trace_mode(w.jobs[j].s);
+        if (m == kTraceBinary) mode = kTraceBinary;
+        else if (m == kTraceWideTlas && mode == kTraceWide) mode = kTraceWideTlas;
+    }
     if (timer && (e = stage_timer_reserve(*timer, timer->used + 2 + 3 * (int)w.nb + 1)) != cudaSuccess) return e;
     auto tb = [&](int stage) {
         if (timer) {
@@ -172,15 +176,17 @@ cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, 
     te();
     for (uint32_t b = 0; b < w.nb; ++b) {
         tb(0);
-        if (wide) wfm_extend<true><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
-        else wfm_extend<false><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
+        if (mode == kTraceWide) wfm_extend<kTraceWide><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
+        else if (mode == kTraceWideTlas) wfm_extend<kTraceWideTlas><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
+        else wfm_extend<kTraceBinary><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
         te();
         tb(1);
         wfm_shade<<<w.blk[1][w.njobs], 128, 0, stream>>>(st, b);
         te();
         tb(2);
-        if (wide) wfm_shadow<true><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
-        else wfm_shadow<false><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
+        if (mode == kTraceWide) wfm_shadow<kTraceWide><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
+        else if (mode == kTraceWideTlas) wfm_shadow<kTraceWideTlas><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
+        else wfm_shadow<kTraceBinary><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
         te();
     }
     tb(3);

@@ -32,16 +32,18 @@ struct SingleWave {
 __global__ void __launch_bounds__(128) wf_camera(const __grid_constant__ SingleWave w, WfState st) {
     camera_body(w, st);
 }
-template <bool kWide>
-__global__ void __launch_bounds__(128, GBRT_TRACE_MINB) wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
-    extend_body<kWide>(w, st, b);
+template <int kMode>
+__global__ void __launch_bounds__(128, trace_minb(kMode))
+    wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
+    extend_body<kMode>(w, st, b);
 }
 __global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     shade_body(w, st, b);
 }
-template <bool kWide>
-__global__ void __launch_bounds__(128, GBRT_TRACE_MINB) wf_shadow(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
-    shadow_body<kWide>(w, st, b);
+template <int kMode>
+__global__ void __launch_bounds__(128, trace_minb(kMode))
+    wf_shadow(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
+    shadow_body<kMode>(w, st, b);
 }
 __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleWave w, WfState st) {
     finish_body(w, st);
@@ -80,9 +82,9 @@ cudaError_t grids(Grid& g) {
     if (g.dev == dev) return cudaSuccess;
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend<true>, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<true>, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
     g.shadow = sms * (bh > 0 ? bh : 1);
@@ -171,7 +173,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
     J.flags = ubo.fully_opaque ? GBRT_RAY_OPAQUE : 0u;
     J.tfar = ubo.orthographic_fov_dis > 0.0f ? 100000.0f : 10000.0f;
     J.path0 = 0;
-    const bool wide = s.cw_nodes != nullptr;
+    const int mode = trace_mode(s);
     // waves: k samples of a pixel range, k * npw <= cap
     for (uint32_t px0 = 0; px0 < npix;) {
         const uint32_t npw = npix - px0 < cap ? npix - px0 : cap;
@@ -187,15 +189,17 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
             te();
             for (uint32_t b = 0; b < nb; ++b) {
                 tb(0);
-                if (wide) wf_extend<true><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
-                else wf_extend<false><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
+                if (mode == kTraceWide) wf_extend<kTraceWide><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
+                else if (mode == kTraceWideTlas) wf_extend<kTraceWideTlas><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
+                else wf_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
                 te();
                 tb(1);
                 wf_shade<<<g_grid.shade, 128, 0, stream>>>(w, st, b);
                 te();
                 tb(2);
-                if (wide) wf_shadow<true><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
-                else wf_shadow<false><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
+                if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
+                else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
+                else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
                 te();
             }
             tb(3);
