@@ -479,6 +479,61 @@ int gbrt_job_wait(gbrt_ctx* ctx, uint64_t job_id, uint32_t timeout_ms, gbrt_job_
 int gbrt_jobs_configure(gbrt_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t policy);
 
 /* ------------------------------------------------------------------------ */
+/* Neural radiance cache                                                     */
+/* ------------------------------------------------------------------------ */
+/* No reference counterpart (the reference path traces every bounce).  A
+ * radiance cache maps a world position to outgoing radiance through a
+ * multiresolution hash-grid encoding (16 levels x 2^log2_table entries x 2
+ * features) and an MLP 32 -> 5 x 64 (ReLU) -> 3, trained online on path
+ * suffixes.  Queries run the MLP on tensor cores in BF16 with FP32
+ * accumulation; training runs in FP32 with Adam (b1 0.9, b2 0.99, eps 1e-15)
+ * on the loss mean((y - t)^2 / (y^2 + 0.01)) (y not differentiated in the
+ * denominator).  Positions are normalised to [box_lo, box_hi]. */
+typedef struct gbrt_nrc gbrt_nrc;
+
+typedef struct gbrt_nrc_config {
+    uint32_t log2_table;       /* entries per level = 2^log2_table (19 = the 32 MiB FP16 table) */
+    uint32_t base_resolution;  /* coarsest level scale + 1 (16) */
+    float growth;              /* per-level scale factor (about 1.45 for 16 -> 4096) */
+    float learning_rate;       /* Adam step size (1e-2) */
+    float box_lo[3], box_hi[3];
+    uint64_t seed;             /* parameter initialisation */
+} gbrt_nrc_config;
+
+int gbrt_nrc_create(gbrt_ctx* ctx, const gbrt_nrc_config* cfg, gbrt_nrc** out);
+int gbrt_nrc_destroy(gbrt_nrc* nrc);
+/* FP32 master parameters: mlp = 18,624 weights (W0 [64][32], W1..W4
+ * [64][64], W5 [3][64], each [out][in]); grid = 16 * 2^log2_table * 2
+ * features.  upload != 0 copies host -> device, else device -> host; either
+ * pointer may be NULL. */
+int gbrt_nrc_params(gbrt_nrc* nrc, float* mlp, float* grid, int upload);
+/* n queries: pos4 = (x, y, z, payload) per query, out4 = (r, g, b, payload). */
+int gbrt_nrc_query(gbrt_nrc* nrc, const float* pos4, uint32_t n, float* out4);
+/* Loss and gradients of one batch (pos4, target4 = (r, g, b, -)); step != 0
+ * then applies one Adam step.  loss / grad_mlp / grad_grid may be NULL. */
+int gbrt_nrc_train(gbrt_nrc* nrc, const float* pos4, const float* target4, uint32_t n, int step, float* loss,
+                   float* grad_mlp, float* grad_grid);
+
+/* A frame rendered with the cache (wavefront form).  A path's cache vertex
+ * is its first hit after the camera hit whose material roughness factor
+ * (1 - glossiness for specular-glossiness) is >= min_roughness.  Render
+ * paths stop there and add throughput x cache(position); about
+ * train_samples paths per frame (chosen by a hash of pixel and sample) trace
+ * on as plain path tracing and give one training sample each: the radiance
+ * gathered from their cache vertex on, divided by the throughput reaching
+ * it.  After the frame, train_steps Adam steps on those samples; *loss (may
+ * be NULL) gets the loss of the last step.  disabled = 1: no path stops (the image is
+ * plain path tracing; the cache still trains). */
+typedef struct gbrt_nrc_render_opts {
+    float min_roughness;
+    uint32_t train_samples;
+    uint32_t train_steps;
+    uint32_t disabled;
+} gbrt_nrc_render_opts;
+int gbrt_render_nrc(gbrt_scene* scene, gbrt_nrc* nrc, const gbrt_ubo* ubo, gbrt_accum* accum, uint8_t* out_rgba8,
+                    gbrt_stats* stats, const gbrt_nrc_render_opts* opts, float* loss);
+
+/* ------------------------------------------------------------------------ */
 /* Device memory helpers (for callers without a CUDA runtime of their own)  */
 /* ------------------------------------------------------------------------ */
 int gbrt_device_alloc(gbrt_ctx* ctx, uint64_t bytes, void** d_ptr);

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "kernels.h"
+#include "nrc.cuh"
 
 using gbrt::DevScene;
 using gbrt::DeviceCounters;
@@ -129,6 +130,14 @@ int build_all(gbrt_scene* s);
 // Linear-blend skinning of the scene's bind-pose vertices, then build_all.
 int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin);
 void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t launches);
+
+// nrc.cu: cache queries and one training step on device arrays (stream-ordered).
+cudaError_t nrc_query_device(gbrt_nrc* r, const float4* q, uint32_t n, float4* out, cudaStream_t st);
+// Same with the query count read on the device (*n_dev, at most n_max).
+cudaError_t nrc_query_counted(gbrt_nrc* r, const float4* q, const uint32_t* n_dev, uint32_t n_max, float4* out,
+                              cudaStream_t st);
+cudaError_t nrc_train_device(gbrt_nrc* r, const float4* pos, const float4* target, uint32_t n, cudaStream_t st);
+const gbrt::NrcView& nrc_view(const gbrt_nrc* r);
 
 // jobs.cu: stops the scheduler thread after the queued jobs (ctx destroy).
 void jobs_shutdown(gbrt_ctx* c);

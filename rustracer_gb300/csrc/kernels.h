@@ -84,6 +84,28 @@ void wave_ring_free(WaveRing& r);
 // Waits until the next slot is free and returns it for filling.
 cudaError_t wave_acquire(WaveRing& r, WaveDesc** slot);
 
+// Radiance-cache state of a wavefront frame (gbrt_render_nrc).  A path's
+// cache vertex is its first hit at bounce >= 1 whose material roughness is
+// at least min_roughness.  Render paths stop there and take throughput x
+// cache(position); training paths (hash of pixel and sample below
+// train_thresh / 65536) trace on and yield one sample: position -> the
+// radiance their suffix gathered from that vertex divided by the throughput
+// that reached it.
+struct NrcWave {
+    float4* query;      // [cap] (position, queue word) of stopped render paths, per bounce
+    float4* qout;       // [cap] cache output for them
+    float4* snap_pos;   // [cap] per path: the training vertex (w = 1 once set)
+    float4* snap_rad;   // [cap] radiance before it
+    float4* snap_tp;    // [cap] throughput reaching it
+    float4* train_pos;  // [train_max] training samples
+    float4* train_tgt;
+    uint32_t* counts;   // [b] queries of bounce b, [32] training samples
+    uint32_t train_max;
+    uint32_t train_thresh;
+    float min_roughness;
+    uint32_t disabled;  // 1: no path stops at the cache (plain path tracing plus training samples)
+};
+
 // CUDA-event pairs around every wavefront launch, grouped by stage
 // (0 extend, 1 shade, 2 shadow, 3 other).  Events are created on demand and
 // reused across frames.
@@ -106,8 +128,11 @@ cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, 
 // Accumulate + tone map of one finished frame (rgen:132-166).
 cudaError_t launch_resolve(const gbrt_ubo& ubo, const RenderOut& out, const float4* frame_sum, cudaStream_t stream);
 // A whole frame of one scene: waves of at most st.cap paths, then resolve.
+// With `nrc` (and `cache`, the gbrt_nrc to query), paths stop at the radiance
+// cache as NrcWave describes.
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
-                             cudaStream_t stream, StageTimer* timer = nullptr);
+                             cudaStream_t stream, StageTimer* timer = nullptr, const NrcWave* nrc = nullptr,
+                             gbrt_nrc* cache = nullptr);
 // Ray queries through the persistent world traversal (8-wide when built);
 // `work` is one device word used as the fetch cursor.
 cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays, uint32_t n, uint32_t flags,

@@ -1,0 +1,734 @@
+// nrc.cu — kernels of the neural radiance cache (layout in nrc.cuh).
+//
+// * nrc_infer_kernel: queries (the path tracer's hot use): FP16 hash-grid
+//   gather, then the MLP on tensor cores (mma.sync m16n8k16, BF16 inputs,
+//   FP32 accumulation).  A warp takes 32 queries; the encoding is written to
+//   shared memory once and read back as A fragments, and every later layer's
+//   A fragments are the previous layer's accumulators after ReLU and BF16
+//   packing, so activations never leave registers.  Weights (BF16, rows
+//   padded by 8 to spread the shared-memory banks) are loaded once per block.
+// * nrc_train_kernel: one thread per training sample, FP32: encoding from
+//   the FP32 master table, forward, relative L2 loss (y - t)^2 / (sg(y)^2 +
+//   0.01) averaged over samples and channels, backward to the encoding; the
+//   table gradient is scattered with atomics, activations and pre-activation
+//   gradients are stored for
+// * nrc_wgrad_kernel: dW_l = sum over samples of dZ_{l+1} H_l^T, split over
+//   the batch, atomics into the FP32 gradient;
+// * nrc_adam_grid_kernel / nrc_adam_mlp_kernel: Adam on the FP32 masters,
+//   rewriting the FP16 / BF16 copies the queries read.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "api_internal.h"
+#include "nrc.cuh"
+
+using namespace gbrt;
+
+namespace gbrt {
+
+namespace {
+
+constexpr int kActStride = kNrcIn + kNrcHiddenLayers * kNrcHidden;    // 352: H0 | H1..H5
+constexpr int kGradStride = kNrcHiddenLayers * kNrcHidden + 8;        // 328: dZ1..dZ5 | dY (3, padded)
+constexpr int kPadK = 8;                                               // BF16 row padding
+
+// offsets of layer l in the padded BF16 copy
+__host__ __device__ constexpr int bf16_off(int l) {
+    return l == 0 ? 0 : kNrcHidden * (kNrcIn + kPadK) + (l - 1) * kNrcHidden * (kNrcHidden + kPadK);
+}
+constexpr int kBf16Padded = bf16_off(5) + 8 * (kNrcHidden + kPadK);  // 21568
+__host__ __device__ constexpr int f32_off(int l) { return l == 0 ? 0 : kNrcWh + (l - 1) * kNrcHidden * kNrcHidden; }
+__host__ __device__ constexpr int in_dim(int l) { return l == 0 ? kNrcIn : kNrcHidden; }
+__host__ __device__ constexpr int out_dim(int l) { return l == 5 ? kNrcOut : kNrcHidden; }
+
+GB_D void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+GB_D uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// One layer on a warp's 32 rows: acc[m][nt] = A[m] (32 x K) * W^T (K x 8*NT).
+template <int K, int NT>
+GB_D void mlp_layer(const __nv_bfloat16* w, const uint32_t (&a)[2][4][4], float (&acc)[2][8][4], int g, int t) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.0f;
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks) {
+#pragma unroll
+        for (int n = 0; n < NT; ++n) {
+            const __nv_bfloat16* row = w + (n * 8 + g) * (K + kPadK) + ks * 16 + t * 2;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
+            mma_bf16(acc[0][n], a[0][ks], b0, b1);
+            mma_bf16(acc[1][n], a[1][ks], b0, b1);
+        }
+    }
+}
+
+// Accumulators of a 64-wide layer -> ReLU -> A fragments of the next layer.
+GB_D void relu_to_a(const float (&acc)[2][8][4], uint32_t (&a)[2][4][4]) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            a[m][j][0] = pack_bf16(fmaxf(acc[m][2 * j][0], 0.0f), fmaxf(acc[m][2 * j][1], 0.0f));
+            a[m][j][1] = pack_bf16(fmaxf(acc[m][2 * j][2], 0.0f), fmaxf(acc[m][2 * j][3], 0.0f));
+            a[m][j][2] = pack_bf16(fmaxf(acc[m][2 * j + 1][0], 0.0f), fmaxf(acc[m][2 * j + 1][1], 0.0f));
+            a[m][j][3] = pack_bf16(fmaxf(acc[m][2 * j + 1][2], 0.0f), fmaxf(acc[m][2 * j + 1][3], 0.0f));
+        }
+}
+
+}  // namespace
+
+// FP16 encoding of one point (32 features).
+GB_D void nrc_encode_h(const NrcView& v, float3 p, float (&x)[kNrcIn]) {
+#pragma unroll
+    for (int l = 0; l < kNrcLevels; ++l) {
+        float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            uint32_t idx;
+            float w;
+            nrc_corner(v, l, p, c, idx, w);
+            const float2 e = __half22float2(v.grid_h[idx]);
+            f0 = fmaf(w, e.x, f0);
+            f1 = fmaf(w, e.y, f1);
+        }
+        x[2 * l] = f0;
+        x[2 * l + 1] = f1;
+    }
+}
+
+constexpr int kInferWarps = 4;
+constexpr int kInRow = kNrcIn + kPadK;  // 40 BF16 per input row
+constexpr size_t kInferSmem = (size_t)kBf16Padded * 2 + (size_t)kInferWarps * 32 * kInRow * 2;
+
+// q[i] = (position, payload); out[i] = (radiance, payload)
+__global__ void __launch_bounds__(128) nrc_infer_kernel(NrcView v, const float4* __restrict__ q, uint32_t n,
+                                                        float4* __restrict__ out, const uint32_t* n_dev) {
+    if (n_dev) n = min(n, *n_dev);
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem);
+    __nv_bfloat16* sin_all = sw + kBf16Padded;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(v.mlp_h);
+        uint4* dst = reinterpret_cast<uint4*>(sw);
+        for (int i = threadIdx.x; i < kBf16Padded / 8; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* sin = sin_all + warp * 32 * kInRow;
+    for (uint32_t base = (blockIdx.x * kInferWarps + warp) * 32u; base < n;
+         base += gridDim.x * kInferWarps * 32u) {
+        const uint32_t i = base + lane;
+        {
+            float x[kNrcIn];
+            const float4 qi = i < n ? q[i] : f4(0.0f, 0.0f, 0.0f, 0.0f);
+            nrc_encode_h(v, nrc_normalise(v, f3(qi)), x);
+#pragma unroll
+            for (int k = 0; k < kNrcIn; k += 2)
+                *reinterpret_cast<uint32_t*>(sin + lane * kInRow + k) = pack_bf16(x[k], x[k + 1]);
+        }
+        __syncwarp();
+        uint32_t a[2][4][4];
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+                const __nv_bfloat16* r0 = sin + (m * 16 + g) * kInRow + ks * 16 + t * 2;
+                const __nv_bfloat16* r1 = r0 + 8 * kInRow;
+                a[m][ks][0] = *reinterpret_cast<const uint32_t*>(r0);
+                a[m][ks][1] = *reinterpret_cast<const uint32_t*>(r1);
+                a[m][ks][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+                a[m][ks][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+            }
+        __syncwarp();
+        float acc[2][8][4];
+        mlp_layer<kNrcIn, 8>(sw + bf16_off(0), a, acc, g, t);
+        relu_to_a(acc, a);
+#pragma unroll
+        for (int l = 1; l < kNrcHiddenLayers; ++l) {
+            mlp_layer<kNrcHidden, 8>(sw + bf16_off(l), a, acc, g, t);
+            relu_to_a(acc, a);
+        }
+        mlp_layer<kNrcHidden, 1>(sw + bf16_off(5), a, acc, g, t);
+        // output columns 0..2: lanes t = 0 (cols 0, 1) and t = 1 (col 2)
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t row = base + m * 16 + g + h * 8;
+                if (row < n) {
+                    float* o = reinterpret_cast<float*>(out + row);
+                    if (t == 0) {
+                        o[0] = acc[m][0][2 * h];
+                        o[1] = acc[m][0][2 * h + 1];
+                    } else if (t == 1) {
+                        o[2] = acc[m][0][2 * h];
+                        o[3] = q[row].w;
+                    }
+                }
+            }
+    }
+}
+
+struct NrcGrad {
+    float* grid;  // [levels * table * 2]
+    float* mlp;   // [kNrcMlpParams]
+    float* act;   // [n][kActStride]
+    float* dz;    // [n][kGradStride]
+    float* loss;  // one word
+};
+
+constexpr size_t kTrainSmem = (size_t)kNrcMlpParams * 4;
+
+__global__ void __launch_bounds__(128) nrc_train_kernel(NrcView v, NrcGrad gr, const float4* __restrict__ pos,
+                                                        const float4* __restrict__ target, uint32_t n, float inv_n) {
+    extern __shared__ float swf[];
+    for (int i = threadIdx.x; i < kNrcMlpParams; i += blockDim.x) swf[i] = v.mlp_w[i];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float loss = 0.0f;
+    if (i < n) {
+        float* A = gr.act + (size_t)i * kActStride;
+        float* D = gr.dz + (size_t)i * kGradStride;
+        const float3 p = nrc_normalise(v, f3(pos[i]));
+        float x[kNrcIn];
+#pragma unroll
+        for (int l = 0; l < kNrcLevels; ++l) {
+            float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint32_t idx;
+                float w;
+                nrc_corner(v, l, p, c, idx, w);
+                f0 = fmaf(w, v.grid_w[2 * idx], f0);
+                f1 = fmaf(w, v.grid_w[2 * idx + 1], f1);
+            }
+            x[2 * l] = f0;
+            x[2 * l + 1] = f1;
+        }
+        for (int k = 0; k < kNrcIn; ++k) A[k] = x[k];
+        float h[kNrcHidden];
+        for (int o = 0; o < kNrcHidden; ++o) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kNrcIn; ++k) s = fmaf(swf[o * kNrcIn + k], x[k], s);
+            h[o] = fmaxf(s, 0.0f);
+            A[kNrcIn + o] = h[o];
+        }
+        for (int l = 1; l < kNrcHiddenLayers; ++l) {
+            const float* W = swf + f32_off(l);
+            float hn[kNrcHidden];
+            for (int o = 0; o < kNrcHidden; ++o) {
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < kNrcHidden; ++k) s = fmaf(W[o * kNrcHidden + k], h[k], s);
+                hn[o] = fmaxf(s, 0.0f);
+            }
+            for (int o = 0; o < kNrcHidden; ++o) {
+                h[o] = hn[o];
+                A[kNrcIn + l * kNrcHidden + o] = hn[o];
+            }
+        }
+        const float4 tg = target[i];
+        const float tc[3] = {tg.x, tg.y, tg.z};
+        float dy[3];
+        for (int c = 0; c < 3; ++c) {
+            float y = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kNrcHidden; ++k) y = fmaf(swf[kNrcW5 + c * kNrcHidden + k], h[k], y);
+            const float d = y - tc[c], den = y * y + 0.01f;
+            loss += d * d / den;
+            dy[c] = 2.0f * d / den * (inv_n / 3.0f);
+            D[5 * kNrcHidden + c] = dy[c];
+        }
+        // backward: dZ5 = (W5^T dy) * [H5 > 0]
+        float dz[kNrcHidden];
+        for (int k = 0; k < kNrcHidden; ++k) {
+            const float s = swf[kNrcW5 + k] * dy[0] + swf[kNrcW5 + kNrcHidden + k] * dy[1] +
+                            swf[kNrcW5 + 2 * kNrcHidden + k] * dy[2];
+            dz[k] = h[k] > 0.0f ? s : 0.0f;
+            D[4 * kNrcHidden + k] = dz[k];
+        }
+        // hidden layers l = 4..1: dZ_l = (W_l^T dZ_{l+1}) * [H_l > 0]
+        for (int l = kNrcHiddenLayers - 1; l >= 1; --l) {
+            const float* W = swf + f32_off(l);
+            const float* Hl = A + kNrcIn + (l - 1) * kNrcHidden;
+            float dp[kNrcHidden];
+            for (int k = 0; k < kNrcHidden; ++k) {
+                float s = 0.0f;
+#pragma unroll 8
+                for (int o = 0; o < kNrcHidden; ++o) s = fmaf(W[o * kNrcHidden + k], dz[o], s);
+                dp[k] = Hl[k] > 0.0f ? s : 0.0f;
+            }
+            for (int k = 0; k < kNrcHidden; ++k) {
+                dz[k] = dp[k];
+                D[(l - 1) * kNrcHidden + k] = dp[k];
+            }
+        }
+        // encoding gradient dH0 = W0^T dZ1, scattered to the table corners
+        float dx[kNrcIn];
+        for (int k = 0; k < kNrcIn; ++k) {
+            float s = 0.0f;
+#pragma unroll 8
+            for (int o = 0; o < kNrcHidden; ++o) s = fmaf(swf[o * kNrcIn + k], dz[o], s);
+            dx[k] = s;
+        }
+        for (int l = 0; l < kNrcLevels; ++l)
+            for (int c = 0; c < 8; ++c) {
+                uint32_t idx;
+                float w;
+                nrc_corner(v, l, p, c, idx, w);
+                atomicAdd(&gr.grid[2 * idx], w * dx[2 * l]);
+                atomicAdd(&gr.grid[2 * idx + 1], w * dx[2 * l + 1]);
+            }
+    }
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xFFFFFFFFu, loss, o);
+    if ((threadIdx.x & 31) == 0 && loss != 0.0f) atomicAdd(gr.loss, loss * inv_n / 3.0f);
+}
+
+// dW_l[o][k] = sum_m D[m][dz of layer l's output o] * A[m][input k of layer l];
+// block (split, layer), 256 threads, samples [split*chunk, ...) in tiles of 32.
+__global__ void __launch_bounds__(256) nrc_wgrad_kernel(const float* __restrict__ act, const float* __restrict__ dz,
+                                                        uint32_t n, uint32_t chunk, float* grad) {
+    const int l = blockIdx.y;
+    const int K = in_dim(l), O = out_dim(l);
+    const int aoff = l == 0 ? 0 : kNrcIn + (l - 1) * kNrcHidden;
+    const int doff = l == 5 ? 5 * kNrcHidden : l * kNrcHidden;
+    __shared__ float sa[32][kNrcHidden + 1], sd[32][kNrcHidden + 1];
+    float accv[16];
+    for (int e = 0; e < 16; ++e) accv[e] = 0.0f;
+    const uint32_t m0 = blockIdx.x * chunk, m1 = min(n, m0 + chunk);
+    for (uint32_t mb = m0; mb < m1; mb += 32) {
+        for (int e = threadIdx.x; e < 32 * kNrcHidden; e += blockDim.x) {
+            const int r = e / kNrcHidden, c = e % kNrcHidden;
+            const uint32_t m = mb + r;
+            sa[r][c] = (m < m1 && c < K) ? act[(size_t)m * kActStride + aoff + c] : 0.0f;
+            sd[r][c] = (m < m1 && c < O) ? dz[(size_t)m * kGradStride + doff + c] : 0.0f;
+        }
+        __syncthreads();
+        for (int e = 0; e < 16; ++e) {
+            const int idx = threadIdx.x + e * 256;  // (o, k) flattened, o * 64 + k
+            const int o = idx >> 6, k = idx & 63;
+            float s = accv[e];
+#pragma unroll 8
+            for (int r = 0; r < 32; ++r) s = fmaf(sd[r][o], sa[r][k], s);
+            accv[e] = s;
+        }
+        __syncthreads();
+    }
+    for (int e = 0; e < 16; ++e) {
+        const int idx = threadIdx.x + e * 256;
+        const int o = idx >> 6, k = idx & 63;
+        if (o < O && k < K && accv[e] != 0.0f) atomicAdd(&grad[f32_off(l) + o * K + k], accv[e]);
+    }
+}
+
+struct AdamCfg {
+    float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
+};
+
+GB_D float adam_one(float& w, float g, float& m, float& v, const AdamCfg& a) {
+    m = a.b1 * m + (1.0f - a.b1) * g;
+    v = a.b2 * v + (1.0f - a.b2) * g * g;
+    w = w - a.lr * (m * a.c1) / (sqrtf(v * a.c2) + a.eps);
+    return w;
+}
+
+// Adam over the table: thread i updates entry i (both features) and its
+// half2 copy.
+__global__ void nrc_adam_grid_kernel(float2* w, const float2* g, float2* m, float2* v, uint32_t n, AdamCfg a,
+                                     __half2* grid_h) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 wi = w[i], mi = m[i], vi = v[i];
+    const float2 gi = g[i];
+    adam_one(wi.x, gi.x, mi.x, vi.x, a);
+    adam_one(wi.y, gi.y, mi.y, vi.y, a);
+    w[i] = wi;
+    m[i] = mi;
+    v[i] = vi;
+    grid_h[i] = __floats2half2_rn(wi.x, wi.y);
+}
+
+// Adam over the MLP and its padded BF16 copy.
+__global__ void nrc_adam_mlp_kernel(float* w, const float* g, float* m, float* v, AdamCfg a, __nv_bfloat16* mlp_h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNrcMlpParams) return;
+    float wi = w[i], mi = m[i], vi = v[i];
+    adam_one(wi, g[i], mi, vi, a);
+    w[i] = wi;
+    m[i] = mi;
+    v[i] = vi;
+    int l = 0;
+    while (l < 5 && i >= f32_off(l + 1)) ++l;
+    const int K = in_dim(l), r = (i - f32_off(l)) / K, c = (i - f32_off(l)) % K;
+    mlp_h[bf16_off(l) + r * (K + kPadK) + c] = __float2bfloat16_rn(wi);
+}
+
+// FP16 / BF16 copies of the masters (after init or a parameter upload).
+__global__ void nrc_copy_kernel(const float* grid_w, uint32_t ngrid2, __half2* grid_h, const float* mlp_w,
+                                __nv_bfloat16* mlp_h) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ngrid2) grid_h[i] = __floats2half2_rn(grid_w[2 * i], grid_w[2 * i + 1]);
+    if (i < (uint32_t)kNrcMlpParams) {
+        int l = 0;
+        while (l < 5 && (int)i >= f32_off(l + 1)) ++l;
+        const int K = in_dim(l), r = ((int)i - f32_off(l)) / K, c = ((int)i - f32_off(l)) % K;
+        mlp_h[bf16_off(l) + r * (K + kPadK) + c] = __float2bfloat16_rn(mlp_w[i]);
+    }
+}
+
+}  // namespace gbrt
+
+// --- host side ---------------------------------------------------------------
+using gbrt_host::DevBuf;
+using gbrt_host::DeviceGuard;
+using gbrt_host::fail;
+
+struct gbrt_nrc {
+    gbrt_ctx* ctx = nullptr;
+    DevBuf f_query, f_qout, f_snap_pos, f_snap_rad, f_snap_tp, f_train_pos, f_train_tgt, f_counts;
+    uint32_t f_cap = 0, f_train_max = 0;
+    gbrt_nrc_config cfg{};
+    NrcView view{};
+    uint32_t nentries = 0;  // levels * table
+    DevBuf grid_w, grid_h, grid_g, grid_m, grid_v;
+    DevBuf mlp_w, mlp_h, mlp_g, mlp_m, mlp_v;
+    DevBuf act, dz, loss, io_a, io_b;
+    uint32_t step = 0;
+    int infer_blocks = 0;
+};
+
+namespace {
+
+int nrc_setup_view(gbrt_nrc* r) {
+    const gbrt_nrc_config& c = r->cfg;
+    NrcView& v = r->view;
+    v.table = 1u << c.log2_table;
+    for (int l = 0; l < kNrcLevels; ++l) {
+        const double s = (double)c.base_resolution * std::pow((double)c.growth, (double)l) - 1.0;
+        v.lv[l].scale = (float)s;
+        const double res = std::ceil((double)(float)s) + 2.0;
+        v.lv[l].res = res * res * res <= (double)v.table ? (uint32_t)res : 0u;
+    }
+    v.lo = make_float3(c.box_lo[0], c.box_lo[1], c.box_lo[2]);
+    v.inv_ext = make_float3(1.0f / (c.box_hi[0] - c.box_lo[0]), 1.0f / (c.box_hi[1] - c.box_lo[1]),
+                            1.0f / (c.box_hi[2] - c.box_lo[2]));
+    v.grid_w = r->grid_w.as<float>();
+    v.grid_h = r->grid_h.as<__half2>();
+    v.mlp_w = r->mlp_w.as<float>();
+    v.mlp_h = r->mlp_h.as<__nv_bfloat16>();
+    return GBRT_OK;
+}
+
+cudaError_t nrc_refresh_copies(gbrt_nrc* r, cudaStream_t st) {
+    const uint32_t n = std::max<uint32_t>(r->nentries, kNrcMlpParams);
+    nrc_copy_kernel<<<(n + 255) / 256, 256, 0, st>>>(r->grid_w.as<float>(), r->nentries, r->grid_h.as<__half2>(),
+                                                     r->mlp_w.as<float>(), r->mlp_h.as<__nv_bfloat16>());
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_reserve_batch(gbrt_nrc* r, uint32_t n) {
+    cudaError_t e = r->act.reserve((size_t)n * kActStride * 4);
+    if (e == cudaSuccess) e = r->dz.reserve((size_t)n * kGradStride * 4);
+    return e;
+}
+
+// Gradients of the mean loss over n samples (device arrays) into grid_g / mlp_g.
+cudaError_t nrc_gradients(gbrt_nrc* r, const float4* pos, const float4* target, uint32_t n, cudaStream_t st) {
+    cudaError_t e = nrc_reserve_batch(r, n);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(r->grid_g.p, 0, r->grid_g.bytes, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(r->mlp_g.p, 0, r->mlp_g.bytes, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(r->loss.p, 0, 4, st)) != cudaSuccess) return e;
+    NrcGrad g{r->grid_g.as<float>(), r->mlp_g.as<float>(), r->act.as<float>(), r->dz.as<float>(), r->loss.as<float>()};
+    nrc_train_kernel<<<(n + 127) / 128, 128, kTrainSmem, st>>>(r->view, g, pos, target, n, 1.0f / (float)n);
+    const uint32_t chunk = 1024, splits = (n + chunk - 1) / chunk;
+    nrc_wgrad_kernel<<<dim3(splits, 6), 256, 0, st>>>(r->act.as<float>(), r->dz.as<float>(), n, chunk,
+                                                      r->mlp_g.as<float>());
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_adam(gbrt_nrc* r, cudaStream_t st) {
+    ++r->step;
+    AdamCfg a;
+    a.b1 = 0.9f;
+    a.b2 = 0.99f;
+    a.eps = 1e-15f;
+    a.c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)r->step)));
+    a.c2 = (float)(1.0 / (1.0 - std::pow(0.99, (double)r->step)));
+    a.lr = r->cfg.learning_rate;
+    const uint32_t ne = r->nentries;
+    nrc_adam_grid_kernel<<<(ne + 255) / 256, 256, 0, st>>>(r->grid_w.as<float2>(), r->grid_g.as<float2>(),
+                                                          r->grid_m.as<float2>(), r->grid_v.as<float2>(), ne, a,
+                                                          r->grid_h.as<__half2>());
+    nrc_adam_mlp_kernel<<<(kNrcMlpParams + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_g.as<float>(),
+                                                                     r->mlp_m.as<float>(), r->mlp_v.as<float>(), a,
+                                                                     r->mlp_h.as<__nv_bfloat16>());
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+namespace gbrt_host {
+
+namespace {
+// Shared-memory opt-in of the two kernels above 48 KB and the query grid.
+cudaError_t nrc_kernel_setup(gbrt_nrc* r) {
+    if (!r->infer_blocks) {
+        cudaError_t e = cudaFuncSetAttribute(nrc_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kInferSmem);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
+        if (e != cudaSuccess) return e;
+        int sms = 0, per = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, nrc_infer_kernel, 128, kInferSmem);
+        r->infer_blocks = sms * std::max(per, 1);
+    }
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t nrc_query_device(gbrt_nrc* r, const float4* q, uint32_t n, float4* out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = nrc_kernel_setup(r);
+    if (e != cudaSuccess) return e;
+    const uint32_t need = (n + kInferWarps * 32 - 1) / (kInferWarps * 32);
+    nrc_infer_kernel<<<std::min<uint32_t>(need, (uint32_t)r->infer_blocks), 128, kInferSmem, st>>>(r->view, q, n, out,
+                                                                                                   nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_query_counted(gbrt_nrc* r, const float4* q, const uint32_t* n_dev, uint32_t n_max, float4* out,
+                              cudaStream_t st) {
+    cudaError_t e = nrc_kernel_setup(r);
+    if (e != cudaSuccess) return e;
+    nrc_infer_kernel<<<r->infer_blocks, 128, kInferSmem, st>>>(r->view, q, n_max, out, n_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t nrc_train_device(gbrt_nrc* r, const float4* pos, const float4* target, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = nrc_kernel_setup(r);
+    if (e == cudaSuccess) e = nrc_gradients(r, pos, target, n, st);
+    if (e == cudaSuccess) e = nrc_adam(r, st);
+    return e;
+}
+
+const NrcView& nrc_view(const gbrt_nrc* r) { return r->view; }
+
+}  // namespace gbrt_host
+
+using gbrt_host::nrc_query_device;
+
+extern "C" {
+
+int gbrt_nrc_create(gbrt_ctx* c, const gbrt_nrc_config* cfg, gbrt_nrc** out) {
+    if (!c || !cfg || !out) return fail(c, GBRT_E_INVALID, "NULL argument");
+    *out = nullptr;
+    if (cfg->log2_table < 8 || cfg->log2_table > 24 || cfg->base_resolution < 2 || !(cfg->growth >= 1.0f) ||
+        !(cfg->learning_rate > 0.0f))
+        return fail(c, GBRT_E_INVALID, "bad radiance-cache configuration");
+    for (int k = 0; k < 3; ++k)
+        if (!(cfg->box_hi[k] > cfg->box_lo[k])) return fail(c, GBRT_E_INVALID, "empty radiance-cache box");
+    DeviceGuard g(c->device);
+    auto r = new (std::nothrow) gbrt_nrc();
+    if (!r) return fail(c, GBRT_E_OOM, "host allocation failed");
+    r->ctx = c;
+    r->cfg = *cfg;
+    r->nentries = (uint32_t)kNrcLevels << cfg->log2_table;
+    const size_t ng = (size_t)r->nentries * 2;
+    cudaError_t e = cudaSuccess;
+    for (DevBuf* b : {&r->grid_w, &r->grid_g, &r->grid_m, &r->grid_v})
+        if (e == cudaSuccess) e = b->alloc(ng * 4);
+    if (e == cudaSuccess) e = r->grid_h.alloc(ng * 2);
+    for (DevBuf* b : {&r->mlp_w, &r->mlp_g, &r->mlp_m, &r->mlp_v})
+        if (e == cudaSuccess) e = b->alloc(kNrcMlpParams * 4);
+    if (e == cudaSuccess) e = r->mlp_h.alloc(kBf16Padded * 2);
+    if (e == cudaSuccess) e = r->loss.alloc(4);
+    if (e != cudaSuccess) {
+        delete r;
+        return gbrt_host::cuda_fail(c, e, "radiance-cache buffers");
+    }
+    nrc_setup_view(r);
+    // seeded init: table U(-1e-4, 1e-4), weights U(-sqrt(6 / fan_in), +)
+    std::mt19937_64 rng(cfg->seed);
+    std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+    std::vector<float> hw(ng);
+    for (auto& x : hw) x = (u01(rng) * 2.0f - 1.0f) * 1e-4f;
+    std::vector<float> hm(kNrcMlpParams);
+    for (int l = 0; l < 6; ++l) {
+        const float b = std::sqrt(6.0f / (float)in_dim(l));
+        for (int i = 0; i < in_dim(l) * out_dim(l); ++i) hm[f32_off(l) + i] = (u01(rng) * 2.0f - 1.0f) * b;
+    }
+    cudaStream_t st = c->stream;
+    e = cudaMemcpyAsync(r->grid_w.p, hw.data(), ng * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r->mlp_w.p, hm.data(), kNrcMlpParams * 4, cudaMemcpyHostToDevice, st);
+    for (DevBuf* b : {&r->grid_m, &r->grid_v, &r->mlp_m, &r->mlp_v})
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->p, 0, b->bytes, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->mlp_h.p, 0, r->mlp_h.bytes, st);
+    if (e == cudaSuccess) e = nrc_refresh_copies(r, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        delete r;
+        return gbrt_host::cuda_fail(c, e, "radiance-cache init");
+    }
+    *out = r;
+    return GBRT_OK;
+}
+
+int gbrt_nrc_destroy(gbrt_nrc* r) {
+    if (!r) return GBRT_OK;
+    DeviceGuard g(r->ctx->device);
+    cudaStreamSynchronize(r->ctx->stream);
+    delete r;
+    return GBRT_OK;
+}
+
+int gbrt_nrc_params(gbrt_nrc* r, float* mlp, float* grid, int upload) {
+    if (!r) return GBRT_E_INVALID;
+    gbrt_ctx* c = r->ctx;
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t ng = (size_t)r->nentries * 2 * 4;
+    const cudaMemcpyKind k = upload ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    if (mlp) CU(c, cudaMemcpyAsync(upload ? r->mlp_w.p : mlp, upload ? (void*)mlp : r->mlp_w.p, kNrcMlpParams * 4, k, st), "params");
+    if (grid) CU(c, cudaMemcpyAsync(upload ? r->grid_w.p : grid, upload ? (void*)grid : r->grid_w.p, ng, k, st), "params");
+    if (upload) CU(c, nrc_refresh_copies(r, st), "copies");
+    CU(c, cudaStreamSynchronize(st), "sync");
+    return GBRT_OK;
+}
+
+int gbrt_nrc_query(gbrt_nrc* r, const float* pos4, uint32_t n, float* out4) {
+    if (!r) return GBRT_E_INVALID;
+    gbrt_ctx* c = r->ctx;
+    if (n && (!pos4 || !out4)) return fail(c, GBRT_E_INVALID, "NULL argument");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CU(c, r->io_a.reserve((size_t)n * 16), "cudaMalloc");
+    CU(c, r->io_b.reserve((size_t)n * 16), "cudaMalloc");
+    CU(c, cudaMemcpyAsync(r->io_a.p, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st), "upload");
+    CU(c, nrc_query_device(r, r->io_a.as<float4>(), n, r->io_b.as<float4>(), st), "query");
+    CU(c, cudaMemcpyAsync(out4, r->io_b.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st), "download");
+    CU(c, cudaStreamSynchronize(st), "sync");
+    return GBRT_OK;
+}
+
+int gbrt_nrc_train(gbrt_nrc* r, const float* pos4, const float* target4, uint32_t n, int step, float* loss,
+                   float* grad_mlp, float* grad_grid) {
+    if (!r) return GBRT_E_INVALID;
+    gbrt_ctx* c = r->ctx;
+    if (n == 0 || !pos4 || !target4) return fail(c, GBRT_E_INVALID, "empty batch or NULL argument");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CU(c, r->io_a.reserve((size_t)n * 16), "cudaMalloc");
+    CU(c, r->io_b.reserve((size_t)n * 16), "cudaMalloc");
+    CU(c, cudaMemcpyAsync(r->io_a.p, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st), "upload");
+    CU(c, cudaMemcpyAsync(r->io_b.p, target4, (size_t)n * 16, cudaMemcpyHostToDevice, st), "upload");
+    CU(c, gbrt_host::nrc_kernel_setup(r), "radiance-cache kernel setup");
+    CU(c, nrc_gradients(r, r->io_a.as<float4>(), r->io_b.as<float4>(), n, st), "gradients");
+    if (grad_mlp) CU(c, cudaMemcpyAsync(grad_mlp, r->mlp_g.p, kNrcMlpParams * 4, cudaMemcpyDeviceToHost, st), "download");
+    if (grad_grid)
+        CU(c, cudaMemcpyAsync(grad_grid, r->grid_g.p, (size_t)r->nentries * 8, cudaMemcpyDeviceToHost, st), "download");
+    if (loss) CU(c, cudaMemcpyAsync(loss, r->loss.p, 4, cudaMemcpyDeviceToHost, st), "download");
+    if (step) CU(c, nrc_adam(r, st), "adam");
+    CU(c, cudaStreamSynchronize(st), "sync");
+    return GBRT_OK;
+}
+
+}  // extern "C"
+
+extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t* out_rgba8,
+                               gbrt_stats* stats, const gbrt_nrc_render_opts* opts, float* loss) {
+    using namespace gbrt_host;
+    if (!s || !r) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (!ubo || !acc || !opts) return fail(c, GBRT_E_INVALID, "NULL argument");
+    if (r->ctx != c || acc->ctx != c) return fail(c, GBRT_E_INVALID, "cache or accumulation of another context");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before rendering");
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
+    if (ubo->number_of_samples == 0 || ubo->total_number_of_samples < ubo->number_of_samples)
+        return fail(c, GBRT_E_INVALID, "need 0 < number_of_samples <= total_number_of_samples");
+    if (ubo->number_of_bounces > 31) return fail(c, GBRT_E_INVALID, "the wavefront form handles at most 31 bounces");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const uint32_t W = acc->w, H = acc->h, ns = ubo->number_of_samples;
+    const size_t npix = (size_t)W * H;
+    const uint64_t paths = (uint64_t)npix * ns;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
+    CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
+    const uint32_t tmax = std::max<uint32_t>(opts->train_samples, 1u) * 2u;  // room for the hash's spread
+    if (r->f_cap < cap) {
+        for (DevBuf* b : {&r->f_query, &r->f_qout, &r->f_snap_pos, &r->f_snap_rad, &r->f_snap_tp})
+            CU(c, b->alloc((size_t)cap * sizeof(float4)), "cudaMalloc(cache frame buffers)");
+        r->f_cap = cap;
+    }
+    if (r->f_train_max < tmax) {
+        CU(c, r->f_train_pos.alloc((size_t)tmax * sizeof(float4)), "cudaMalloc(training buffers)");
+        CU(c, r->f_train_tgt.alloc((size_t)tmax * sizeof(float4)), "cudaMalloc(training buffers)");
+        r->f_train_max = tmax;
+    }
+    CU(c, r->f_counts.reserve(64 * sizeof(uint32_t)), "cudaMalloc(counters)");
+    NrcWave nw{};
+    nw.query = r->f_query.as<float4>();
+    nw.qout = r->f_qout.as<float4>();
+    nw.snap_pos = r->f_snap_pos.as<float4>();
+    nw.snap_rad = r->f_snap_rad.as<float4>();
+    nw.snap_tp = r->f_snap_tp.as<float4>();
+    nw.train_pos = r->f_train_pos.as<float4>();
+    nw.train_tgt = r->f_train_tgt.as<float4>();
+    nw.counts = r->f_counts.as<uint32_t>();
+    nw.train_max = r->f_train_max;
+    const double frac = std::min(1.0, (double)opts->train_samples / (double)paths);
+    nw.train_thresh = (uint32_t)std::min(65536.0, std::ceil(frac * 65536.0));
+    nw.min_roughness = opts->min_roughness;
+    nw.disabled = opts->disabled ? 1u : 0u;
+    RenderOut out{};
+    out.width = W;
+    out.height = H;
+    out.accum = acc->buf.as<float4>();
+    out.counters = c->counters.as<DeviceCounters>();
+    if (out_rgba8) {
+        CU(c, c->scratch_img.reserve(npix * 4), "cudaMalloc(image)");
+        out.rgba8 = c->scratch_img.as<uchar4>();
+    }
+    CU(c, cudaMemsetAsync(out.counters, 0, sizeof(DeviceCounters), st), "memset");
+    CU(c, cudaMemsetAsync(nw.counts + 32, 0, sizeof(uint32_t), st), "memset");
+    CU(c, cudaEventRecord(c->ev0, st), "event");
+    CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, nullptr, &nw, r), "wavefront launch");
+    uint32_t ntrain = 0;
+    CU(c, cudaMemcpyAsync(&ntrain, nw.counts + 32, 4, cudaMemcpyDeviceToHost, st), "download");
+    CU(c, cudaStreamSynchronize(st), "render");
+    ntrain = std::min(ntrain, nw.train_max);
+    for (uint32_t k = 0; k < opts->train_steps && ntrain > 0; ++k)
+        CU(c, nrc_train_device(r, nw.train_pos, nw.train_tgt, ntrain, st), "cache training");
+    float lsum = 0.0f;  // loss of the last step
+    if (ntrain > 0 && opts->train_steps) CU(c, cudaMemcpyAsync(&lsum, r->loss.p, 4, cudaMemcpyDeviceToHost, st), "download");
+    CU(c, cudaEventRecord(c->ev1, st), "event");
+    if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
+    DeviceCounters dc;
+    CU(c, cudaMemcpyAsync(&dc, out.counters, sizeof(dc), cudaMemcpyDeviceToHost, st), "download counters");
+    CU(c, cudaStreamSynchronize(st), "render");
+    float ms = 0.0f;
+    CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
+    fill_stats(stats, dc, ms, 0);
+    if (loss) *loss = lsum;
+    if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit");
+    return GBRT_OK;
+}

@@ -8,6 +8,11 @@
 // kernel bodies are in wavefront.cuh; the batched form is wave_multi.cu.
 #include "wavefront.cuh"
 
+namespace gbrt_host {
+cudaError_t nrc_query_counted(gbrt_nrc* r, const float4* q, const uint32_t* n_dev, uint32_t n_max, float4* out,
+                              cudaStream_t st);
+}
+
 namespace gbrt {
 
 namespace {
@@ -47,6 +52,27 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
 }
 __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleWave w, WfState st) {
     finish_body(w, st);
+}
+
+// Radiance-cache forms of shade and finish, and the step that adds
+// throughput x cache output to the paths that stopped at bounce b.
+__global__ void __launch_bounds__(128) wf_shade_nrc(const __grid_constant__ SingleWave w, WfState st, uint32_t b,
+                                                    const __grid_constant__ NrcWave nrc) {
+    shade_body<SingleWave, true>(w, st, b, &nrc);
+}
+__global__ void __launch_bounds__(128) wf_finish_nrc(const __grid_constant__ SingleWave w, WfState st,
+                                                     const __grid_constant__ NrcWave nrc) {
+    finish_body<SingleWave, true>(w, st, &nrc);
+}
+__global__ void __launch_bounds__(256) wf_nrc_apply(WfState st, NrcWave nrc, uint32_t b) {
+    const uint32_t n = nrc.counts[b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 L = nrc.qout[i];
+        const uint32_t pid = __float_as_uint(L.w) & kPidMask;
+        const float4 tp = st.tp[pid], r = st.rad[pid];
+        st.rad[pid] = f4(r.x + tp.x * fmaxf(L.x, 0.0f), r.y + tp.y * fmaxf(L.y, 0.0f), r.z + tp.z * fmaxf(L.z, 0.0f),
+                         r.w);
+    }
 }
 
 // rgen:132-166: accumulate, tone map, write the image.
@@ -145,7 +171,7 @@ cudaError_t launch_resolve(const gbrt_ubo& ubo, const RenderOut& out, const floa
 }
 
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
-                             cudaStream_t stream, StageTimer* timer) {
+                             cudaStream_t stream, StageTimer* timer, const NrcWave* nrc, gbrt_nrc* cache) {
     if (ubo.number_of_bounces > kMaxBounces) return cudaErrorInvalidValue;
     cudaError_t e = grids(g_grid);
     if (e != cudaSuccess) return e;
@@ -182,8 +208,13 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
             const uint32_t k = ns - s0 < kmax ? ns - s0 : kmax;
             J.npaths = k * npw;
             w.S = WaveSeg{0u, 0u, px0, npw, sbase + s0, s0, k, 0u};
-            if (timer && (e = stage_timer_reserve(*timer, timer->used + 3 + 3 * (int)nb)) != cudaSuccess) return e;
+            if (timer && (e = stage_timer_reserve(*timer, timer->used + 3 + 4 * (int)nb)) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(st.counts, 0, kWfCounters * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+            if (nrc) {
+                if ((e = cudaMemsetAsync(nrc->counts, 0, 32 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+                if ((e = cudaMemsetAsync(nrc->snap_pos, 0, (size_t)J.npaths * sizeof(float4), stream)) != cudaSuccess)
+                    return e;
+            }
             tb(3);
             wf_camera<<<(J.npaths + 127) / 128, 128, 0, stream>>>(w, st);
             te();
@@ -194,8 +225,17 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 else wf_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
                 te();
                 tb(1);
-                wf_shade<<<g_grid.shade, 128, 0, stream>>>(w, st, b);
+                if (nrc) wf_shade_nrc<<<g_grid.shade, 128, 0, stream>>>(w, st, b, *nrc);
+                else wf_shade<<<g_grid.shade, 128, 0, stream>>>(w, st, b);
                 te();
+                if (nrc && b >= 1 && !nrc->disabled) {  // cache queries of the paths that stopped here
+                    tb(3);
+                    if ((e = gbrt_host::nrc_query_counted(cache, nrc->query, nrc->counts + b, J.npaths, nrc->qout,
+                                                          stream)) != cudaSuccess)
+                        return e;
+                    wf_nrc_apply<<<g_grid.shade, 256, 0, stream>>>(st, *nrc, b);
+                    te();
+                }
                 tb(2);
                 if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
                 else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
@@ -203,7 +243,8 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 te();
             }
             tb(3);
-            wf_finish<<<(npw + 127) / 128, 128, 0, stream>>>(w, st);
+            if (nrc) wf_finish_nrc<<<(npw + 127) / 128, 128, 0, stream>>>(w, st, *nrc);
+            else wf_finish<<<(npw + 127) / 128, 128, 0, stream>>>(w, st);
             te();
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
             s0 += k;

@@ -164,8 +164,24 @@ GB_D void extend_body(const Wv& w, const WfState& st, uint32_t b) {
 
 // Closest-hit / miss shading and the rest of rgen's bounce loop
 // (RayTracing.rgen:94-128) for the extension queue of bounce b.
-template <class Wv>
-GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b) {
+// Material roughness of a hit as the radiance cache sees it (factor only:
+// metallic-roughness roughness, or 1 - glossiness for specular-glossiness).
+GB_D float hit_roughness(const DevScene& s, uint32_t inst) {
+    const gbrt_priminfo pi = s.prims[s.inst[inst].custom];
+    const gbrt_material_raw& m = s.mats[pi.material_id];
+    return m.workflow == 1u ? 1.0f - m.sg_specular_glossiness_factor[3] : m.roughness_factor;
+}
+
+GB_D uint32_t nrc_train_hash(uint32_t pix, uint32_t sample) {
+    uint32_t h = pix * 0x9E3779B1u ^ (sample + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    return h & 0xFFFFu;
+}
+
+template <class Wv, bool kNrc = false>
+GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* nrc = nullptr) {
     const uint32_t jb = w.block_job(1);
     const WaveJob& J = w.job(jb);
     const DevScene& s = J.s;
@@ -205,7 +221,28 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b) {
             Rp.volume_dis = rad4.w;
             Rp.rngState = make_uint4(P.x, P.y, rg.z, rg.y);
             const uint32_t inst = __float_as_uint(h4.w);
-            if (inst != 0xFFFFFFFFu) {
+            bool cached = false;  // a render path stopping at the radiance cache
+            if constexpr (kNrc) {
+                const bool train = nrc_train_hash(P.pix, P.sg->sample0 + P.j) < nrc->train_thresh;
+                if (b >= 1u && inst != 0xFFFFFFFFu && (train || !nrc->disabled) &&
+                    hit_roughness(s, inst) >= nrc->min_roughness) {
+                    const float3 o = f3(st.ray_o[b & 1][R + q]);
+                    const float3 x = f3(fmaf(h4.x, d.x, o.x), fmaf(h4.x, d.y, o.y), fmaf(h4.x, d.z, o.z));
+                    if (train) {
+                        if (nrc->snap_pos[pid].w == 0.0f) {
+                            nrc->snap_pos[pid] = f4(x, 1.0f);
+                            nrc->snap_rad[pid] = rad4;
+                            nrc->snap_tp[pid] = tp4;
+                        }
+                    } else {
+                        cached = true;
+                        const uint32_t k = atomicAdd(&nrc->counts[b], 1u);
+                        nrc->query[k] = f4(x, __uint_as_float(word));
+                    }
+                }
+            }
+            if (cached) {
+            } else if (inst != 0xFFFFFFFFu) {
                 Hit h;
                 h.t = h4.x;
                 h.u = h4.y;
@@ -223,6 +260,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b) {
             } else {
                 miss_shader(s, ubo, Rp, d);
             }
+            if (!cached) {
             float3 tp = f3(tp4);
             float3 rad = f3(rad4);
             tp_before = tp;
@@ -246,6 +284,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b) {
             st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
+            }
         }
         const uint32_t slot = warp_append(&cnt[kQueue + b + 1], cont);
         if (cont) {
@@ -305,8 +344,8 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b) {
 
 // Per pixel of every segment: add its samples' radiance to the job's frame
 // sum in sample order (the megakernel's per-pixel order), keep the last Ray.t.
-template <class Wv>
-GB_D void finish_body(const Wv& w, const WfState& st) {
+template <class Wv, bool kNrc = false>
+GB_D void finish_body(const Wv& w, const WfState& st, const NrcWave* nrc = nullptr) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.nfin()) return;
     const WaveSeg& sg = w.seg(w.seg_of_fin(i));
@@ -326,6 +365,20 @@ GB_D void finish_body(const Wv& w, const WfState& st) {
         }
         sum += r;
         last_t = st.tp[pid].w;
+        if constexpr (kNrc) {  // training sample: suffix radiance / throughput at the vertex
+            const float4 sp = nrc->snap_pos[pid];
+            if (sp.w != 0.0f) {
+                const float3 r0 = f3(nrc->snap_rad[pid]), t0 = f3(nrc->snap_tp[pid]);
+                const float3 dr = r - r0;
+                const float3 tg = f3(t0.x > 0.0f ? dr.x / t0.x : 0.0f, t0.y > 0.0f ? dr.y / t0.y : 0.0f,
+                                     t0.z > 0.0f ? dr.z / t0.z : 0.0f);
+                const uint32_t k = atomicAdd(&nrc->counts[32], 1u);
+                if (k < nrc->train_max) {
+                    nrc->train_pos[k] = sp;
+                    nrc->train_tgt[k] = f4(tg, 0.0f);
+                }
+            }
+        }
     }
     J.frame_sum[pix] = f4(sum, last_t);
 }

@@ -61,6 +61,12 @@ SIGNATURES = {
     "gbrt_job_poll": (i32, [P, u64, P]),
     "gbrt_job_wait": (i32, [P, u64, u32, P]),
     "gbrt_jobs_configure": (i32, [P, u64, u32]),
+    "gbrt_nrc_create": (i32, [P, P, C.POINTER(P)]),
+    "gbrt_nrc_destroy": (i32, [P]),
+    "gbrt_nrc_params": (i32, [P, P, P, i32]),
+    "gbrt_nrc_query": (i32, [P, P, u32, P]),
+    "gbrt_nrc_train": (i32, [P, P, P, u32, i32, P, P, P]),
+    "gbrt_render_nrc": (i32, [P, P, P, P, P, P, P, P]),
 }
 JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
 POLICY_SRPT, POLICY_FIFO = 0, 1
@@ -189,6 +195,83 @@ class Job:
             return self.info
         info = np.zeros((), T.JOB_INFO)
         return self._finish(self.ctx.L.gbrt_job_wait(self.ctx.h, self.id, timeout_ms, _p(info)), info)
+
+
+class NrcConfig(C.Structure):
+    _fields_ = [("log2_table", C.c_uint32), ("base_resolution", C.c_uint32), ("growth", C.c_float),
+                ("learning_rate", C.c_float), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3),
+                ("seed", C.c_uint64)]
+
+
+class NrcRenderOpts(C.Structure):
+    _fields_ = [("min_roughness", C.c_float), ("train_samples", C.c_uint32), ("train_steps", C.c_uint32),
+                ("disabled", C.c_uint32)]
+
+
+class Nrc:
+    """gbrt_nrc: the neural radiance cache (hash grid + 5x64 MLP)."""
+    MLP_PARAMS = 18624
+
+    def __init__(self, ctx, box_lo, box_hi, log2_table=19, base_resolution=16, growth=1.447, learning_rate=1e-2,
+                 seed=1):
+        self.ctx = ctx
+        self.cfg = NrcConfig(log2_table, base_resolution, growth, learning_rate, (C.c_float * 3)(*box_lo),
+                             (C.c_float * 3)(*box_hi), seed)
+        h = P()
+        ctx.check(ctx.L.gbrt_nrc_create(ctx.h, C.byref(self.cfg), C.byref(h)))
+        self.h = h
+        self.grid_size = 16 * (1 << log2_table) * 2
+
+    def params(self):
+        mlp = np.zeros(self.MLP_PARAMS, np.float32)
+        grid = np.zeros(self.grid_size, np.float32)
+        self.ctx.check(self.ctx.L.gbrt_nrc_params(self.h, _p(mlp), _p(grid), 0))
+        return mlp, grid
+
+    def set_params(self, mlp=None, grid=None):
+        m = None if mlp is None else np.ascontiguousarray(mlp, np.float32)
+        g = None if grid is None else np.ascontiguousarray(grid, np.float32)
+        self.ctx.check(self.ctx.L.gbrt_nrc_params(self.h, _p(m) if m is not None else None,
+                                                  _p(g) if g is not None else None, 1))
+
+    def query(self, pos):
+        q = np.zeros((len(pos), 4), np.float32)
+        q[:, :3] = pos
+        out = np.zeros_like(q)
+        self.ctx.check(self.ctx.L.gbrt_nrc_query(self.h, _p(q), len(q), _p(out)))
+        return out[:, :3]
+
+    def train(self, pos, target, step=True, grads=False):
+        q = np.zeros((len(pos), 4), np.float32)
+        q[:, :3] = pos
+        t = np.zeros((len(pos), 4), np.float32)
+        t[:, :3] = np.asarray(target)[:, :3]
+        loss = np.zeros(1, np.float32)
+        gm = np.zeros(self.MLP_PARAMS, np.float32) if grads else None
+        gg = np.zeros(self.grid_size, np.float32) if grads else None
+        self.ctx.check(self.ctx.L.gbrt_nrc_train(self.h, _p(q), _p(t), len(q), int(step), _p(loss),
+                                                 _p(gm) if grads else None, _p(gg) if grads else None))
+        return (float(loss[0]), gm, gg) if grads else float(loss[0])
+
+    def render(self, scene, ubo, accum, image=True, min_roughness=0.0, train_samples=1 << 16, train_steps=1,
+               disabled=False):
+        """One frame with the cache (gbrt_render_nrc); returns dict(image, stats, loss)."""
+        ubo = np.asarray(ubo, T.UBO).reshape(())
+        img = np.zeros((accum.h_, accum.w, 4), np.uint8) if image else None
+        st = np.zeros((), T.STATS)
+        loss = np.zeros(1, np.float32)
+        opts = NrcRenderOpts(min_roughness, train_samples, train_steps, int(disabled))
+        self.ctx.check(self.ctx.L.gbrt_render_nrc(scene.h, self.h, _p(ubo), accum.h, _p(img) if image else None,
+                                                  _p(st), C.byref(opts), _p(loss)))
+        return dict(image=img, stats=st, loss=float(loss[0]))
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            self.ctx.L.gbrt_nrc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 class Accum:
