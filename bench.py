@@ -454,6 +454,92 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def run_nrc(args):
+    """Radiance cache vs plain path tracing on the city block (about 2M
+    instanced triangles, glossy materials, 16 point lights, sky), 1920x1080,
+    depth 12: device time until the running mean reaches relMSE <= 1e-2
+    against a path-traced reference (--ref-spp samples), relMSE =
+    mean((x - ref)^2 / (ref^2 + 1e-2)).  Plain path tracing adds 4 spp per
+    frame; the cache run adds 1 spp per frame and trains from scratch (its
+    training time is counted)."""
+    from rustracer_gb300 import build, gbrt, workloads as WL
+    build.build()
+    Wn, Hn = (int(x) for x in (args.res or "1920x1080").lower().split("x"))
+    depth, target = 12, 1e-2
+    sd = WL.city_scene()
+    ctx = gbrt.Context(0)
+    sc = gbrt.Scene(ctx, sd)
+    ref_acc = gbrt.Accum(ctx, Wn, Hn)
+    chunk = 32
+    for k in range(0, args.ref_spp, chunk):
+        sc.render(sd.ubo(Wn, Hn, samples=chunk, total=k + chunk, bounces=depth, exposure=1.0, has_sky=True), ref_acc,
+                  image=False, mode=MODES["wavefront"])
+    ref = ref_acc.download()[..., :3] / float(args.ref_spp)
+    den = ref * ref + 1e-2
+
+    def relmse(acc, spp):
+        x = acc.download()[..., :3] / float(spp)
+        return float(np.mean((x - ref) ** 2 / den))
+
+    def curve(step, max_frames):
+        acc = gbrt.Accum(ctx, Wn, Hn)
+        t, spp, pts, reached, rays = 0.0, 0, [], None, 0
+        for f in range(max_frames):
+            ms, r, n = step(acc, spp)
+            t += ms
+            spp += n
+            rays += r
+            e = relmse(acc, spp)
+            pts.append((round(t, 2), spp, round(e, 5)))
+            if e <= target:
+                reached = t
+                break
+        return reached, pts, rays, t
+
+    def pt_step(acc, spp):
+        st = sc.render(sd.ubo(Wn, Hn, samples=4, total=spp + 4, bounces=depth, exposure=1.0, has_sky=True), acc,
+                       image=False, mode=MODES["wavefront"])["stats"]
+        return float(st["device_ms"]), int(st["rays_total"]), 4
+
+    p = sd.vertices["pos"][:, :3]
+    inst = sd.instances["transform"].reshape(-1, 3, 4)
+    corners = np.concatenate([inst[:, :, 3] - 2.0, inst[:, :, 3] + 2.0, p])
+    lo, hi = corners.min(0) - 0.5, corners.max(0) + 0.5
+    cache = gbrt.Nrc(ctx, tuple(map(float, lo)), tuple(map(float, hi)), log2_table=19, learning_rate=1e-3)
+    losses = []
+
+    def nrc_step(acc, spp):
+        r = cache.render(sc, sd.ubo(Wn, Hn, samples=1, total=spp + 1, bounces=depth, exposure=1.0, has_sky=True),
+                         acc, image=False, min_roughness=args.nrc_min_roughness, train_samples=1 << 16,
+                         train_steps=4)
+        losses.append(r["loss"])
+        return float(r["stats"]["device_ms"]), int(r["stats"]["rays_total"]), 1
+
+    with ClockSampler(0) as clk:
+        t_pt, pts_pt, rays_pt, tot_pt = curve(pt_step, args.max_frames)
+        t_nrc, pts_nrc, rays_nrc, tot_nrc = curve(nrc_step, 4 * args.max_frames)
+    clocks = clk.summary()
+    line = {"metric": "time to relMSE <= 1e-2", "value": None if t_nrc is None else t_nrc / 1e3, "unit": "s",
+            "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": tot_nrc, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (cache MLP: bf16 x bf16 -> f32)",
+            "data": "synthetic (seeded city block of instanced boxes and spheres)",
+            "config": {"workload": f"city_nrc_{Wn}x{Hn}_depth{depth}", "instances": int(len(sd.instances)),
+                       "instanced_triangles": int(sd.instanced_triangles), "point_lights": 16, "sky": True,
+                       "reference": f"{args.ref_spp} spp wavefront path tracing (FP32; an FP64 CPU reference at "
+                                    f"this size does not fit the run)",
+                       "cache": {"levels": 16, "table": 1 << 19, "features": 2, "mlp": "32-64x5-3 ReLU",
+                                 "train_samples_per_frame": 1 << 16, "adam_steps_per_frame": 4, "lr": 1e-3,
+                                 "min_roughness": args.nrc_min_roughness}},
+            "plain_pt": {"time_s": None if t_pt is None else t_pt / 1e3, "curve": pts_pt[:: max(1, len(pts_pt) // 24)],
+                         "mrays_per_s": rays_pt / tot_pt / 1e3},
+            "cache": {"time_s": None if t_nrc is None else t_nrc / 1e3,
+                      "curve": pts_nrc[:: max(1, len(pts_nrc) // 24)], "mrays_per_s": rays_nrc / tot_nrc / 1e3,
+                      "final_loss": losses[-1] if losses else None},
+            "speedup": (t_pt / t_nrc) if (t_pt and t_nrc) else None,
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -493,11 +579,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
     ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")
-    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched", "serving"],
+    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched", "serving", "nrc"],
                     help="icosphere: the headline frame; batched: 32 scenes as one batch of jobs; "
                          "serving: Poisson job arrivals with p50/p99 latency")
     ap.add_argument("--jobs", type=int, default=200, help="serving: jobs in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--ref-spp", type=int, default=1024, help="nrc: samples of the reference image")
+    ap.add_argument("--max-frames", type=int, default=200, help="nrc: frame limit of the plain run (x4 for the cache)")
+    ap.add_argument("--nrc-min-roughness", type=float, default=0.25, help="nrc: roughness a cache vertex needs")
     args = ap.parse_args()
     global W, H, SPP, WORKLOAD
     if args.res:
@@ -511,6 +600,8 @@ def main():
         run_batched(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "nrc":
+        run_nrc(args)
     else:
         run_gpu(args)
 

@@ -13,6 +13,9 @@
   triangles, one of them a 64-bone skinned tube animated per job.
 * serving_trace(seed, n, rate): n jobs with Poisson arrivals (rate per
   second) over the pool, resolution and spp log-uniform.
+* city_scene(): the radiance-cache configuration -- 4,000 instances of a box
+  and an icosphere (about 2M instanced triangles), glossy materials, 16
+  point lights and a procedural sky.
 """
 import math
 
@@ -146,3 +149,79 @@ def serving_trace(seed=0, n=200, rate=200.0, nscenes=8, skinned=7, res_lo=256 * 
         jobs.append(dict(arrival=float(t[i]), scene=k, width=w, height=h, spp=max(1, spp),
                          anim_time=float(rng.uniform(0, 6.28)) if k == skinned else None))
     return jobs
+
+
+def _box_mesh():
+    """Unit cube [-0.5, 0.5]^3 with face normals (24 vertices, 12 triangles)."""
+    pos, nrm, idx = [], [], []
+    for axis in range(3):
+        for sgn in (-1.0, 1.0):
+            n = np.zeros(3)
+            n[axis] = sgn
+            u = np.zeros(3)
+            u[(axis + 1) % 3] = 1.0
+            v = np.cross(n, u)
+            base = len(pos)
+            for a, b in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+                pos.append(0.5 * n + 0.5 * a * u + 0.5 * b * v)
+                nrm.append(n)
+            idx += [(base, base + 1, base + 2), (base, base + 2, base + 3)]
+    return np.array(pos, np.float32), np.array(nrm, np.float32), np.array(idx)
+
+
+def sky_faces(size=32, zenith=(70, 120, 220), horizon=(200, 215, 235), ground=(60, 55, 50)):
+    """Procedural cubemap (+X, -X, +Y, -Y, +Z, -Z), RGBA8: a vertical
+    gradient from ground through horizon to zenith."""
+    faces = np.zeros((6, size, size, 4), np.uint8)
+    lerp = lambda a, b, t: (np.asarray(a)[None, None] * (1 - t[..., None]) + np.asarray(b)[None, None] * t[..., None])
+    v = (np.arange(size) + 0.5) / size
+    t = np.repeat(1.0 - v[:, None], size, 1)  # 1 at the top row, 0 at the bottom
+    side = np.where(t[..., None] > 0.5, lerp(horizon, zenith, (t - 0.5) * 2), lerp(ground, horizon, t * 2))
+    for f in (0, 1, 4, 5):
+        faces[f, ..., :3] = side
+    faces[2, ..., :3] = np.asarray(zenith)
+    faces[3, ..., :3] = np.asarray(ground)
+    faces[..., 3] = 255
+    return size, faces.reshape(-1)
+
+
+def city_scene(seed=0, n_boxes=2500, n_spheres=1500, sphere_subdiv=3, nmat=16):
+    """The radiance-cache configuration: a city block of instanced boxes
+    (buildings) and spheres, ~2M instanced triangles, glossy materials
+    (roughness U[0.02, 0.5]), 16 point lights and a procedural sky."""
+    from .scenes import _icosphere
+    rng = np.random.default_rng(500 + seed)
+    b = GeoBuilder()
+    ground_m = b.add_material(lambert((0.35, 0.35, 0.38)))
+    gp = np.array([(-60, 0, -40), (60, 0, -40), (60, 0, 40), (-60, 0, 40)], np.float32)
+    g_ground = b.add_mesh(gp, np.array([[0, 2, 1], [0, 3, 2]]), ground_m, np.tile([0, 1.0, 0], (4, 1)).astype(np.float32))
+    mats = []
+    for _ in range(nmat):
+        m = random_pbr_material(rng, rough_lo=0.02, rough_hi=0.5)
+        mats.append(b.add_material(m))
+    bp, bn, bi = _box_mesh()
+    vb = b.add_vertices(bp, bn)
+    box_geos = [b.add_geometry(vb, len(bp), bi, mats[k]) for k in range(nmat)]
+    sv, sf = _icosphere(sphere_subdiv)
+    vs = b.add_vertices(sv.astype(np.float32), sv.astype(np.float32))
+    sph_geos = [b.add_geometry(vs, len(sv), sf, mats[k]) for k in range(nmat)]
+    geos, xf = [g_ground], [T.IDENTITY34]
+    for _ in range(n_boxes):  # buildings on a jittered grid
+        w, d, h = rng.uniform(1.0, 3.0), rng.uniform(1.0, 3.0), rng.uniform(2.0, 14.0)
+        x, z = rng.uniform(-55, 55), rng.uniform(-35, 35)
+        ang = rng.uniform(0, np.pi / 2)
+        R = _rot((0, 1, 0), ang) @ np.diag([w, h, d])
+        geos.append(box_geos[int(rng.integers(nmat))])
+        xf.append(np.concatenate([R, np.array([[x], [h / 2], [z]])], 1).astype(np.float32).reshape(12))
+    for _ in range(n_spheres):
+        r = rng.uniform(0.3, 1.5)
+        x, y, z = rng.uniform(-55, 55), rng.uniform(r, 16.0), rng.uniform(-35, 35)
+        geos.append(sph_geos[int(rng.integers(nmat))])
+        xf.append(np.concatenate([np.eye(3) * r, np.array([[x], [y], [z]])], 1).astype(np.float32).reshape(12))
+    inst = identity_instances(geos, transforms=xf)
+    plights = [point_light((rng.uniform(-50, 50), rng.uniform(3, 12), rng.uniform(-30, 30)),
+                           tuple(rng.uniform(0.7, 1.0, 3)), rng.uniform(20, 60)) for _ in range(16)]
+    sd = b.finish(instances=inst, plights=np.array(plights, T.LIGHT), skybox=sky_faces(),
+                  camera=dict(eye=(0.0, 28.0, 60.0), direction=(0.0, -0.45, -1.0), fov_deg=55.0), name="city")
+    sd.instanced_triangles = int(n_boxes * 12 + n_spheres * len(sf) + 2)
+    return sd
