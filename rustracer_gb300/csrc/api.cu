@@ -370,6 +370,9 @@ int gbrt_ctx_create(int device, gbrt_ctx** out) {
     };
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
     if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaStreamCreateWithFlags(&c->side.stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+    if ((e = cudaEventCreateWithFlags(&c->side.shaded, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
+    if ((e = cudaEventCreateWithFlags(&c->side.shadowed, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
     if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return bail(e, "event");
     if ((e = cudaEventCreate(&c->tb0)) != cudaSuccess) return bail(e, "event");
     if ((e = cudaEventCreate(&c->tb1)) != cudaSuccess) return bail(e, "event");
@@ -404,6 +407,10 @@ int gbrt_ctx_destroy(gbrt_ctx* c) {
         c->wf_frame.release();
         stage_timer_free(c->timer);
         wave_ring_free(c->ring);
+        if (c->side.stream) cudaStreamSynchronize(c->side.stream);
+        if (c->side.shaded) cudaEventDestroy(c->side.shaded);
+        if (c->side.shadowed) cudaEventDestroy(c->side.shadowed);
+        if (c->side.stream) cudaStreamDestroy(c->side.stream);
         if (c->ev0) cudaEventDestroy(c->ev0);
         if (c->ev1) cudaEventDestroy(c->ev1);
         if (c->tb0) cudaEventDestroy(c->tb0);
@@ -673,7 +680,8 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
         const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
         CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
         const bool timed = opts && (opts->flags & GBRT_RENDER_STAGE_TIMING);
-        CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, timed ? &c->timer : nullptr), "wavefront launch");
+        CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, timed ? &c->timer : nullptr, nullptr, nullptr,
+                               &c->side), "wavefront launch");
         const uint64_t npw = std::min<uint64_t>(npix, cap), k = cap / npw;
         const uint64_t waves = ((npix + npw - 1) / npw) * ((ns + k - 1) / k);
         launches = (uint32_t)(waves * (2 + 3 * ubo->number_of_bounces) + 1);

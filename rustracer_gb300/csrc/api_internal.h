@@ -60,6 +60,7 @@ struct gbrt_ctx {
     gbrt_host::DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums
     WfState wf{};
     WaveRing ring;
+    gbrt::WfSide side;  // shadow-stage stream of single-frame renders
     StageTimer timer;
     std::mutex mu;
     gbrt_host::JobQueue* jobs = nullptr;  // created by the first gbrt_job_submit

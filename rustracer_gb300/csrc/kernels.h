@@ -130,9 +130,16 @@ cudaError_t launch_resolve(const gbrt_ubo& ubo, const RenderOut& out, const floa
 // A whole frame of one scene: waves of at most st.cap paths, then resolve.
 // With `nrc` (and `cache`, the gbrt_nrc to query), paths stop at the radiance
 // cache as NrcWave describes.
+// A second stream for the shadow stage: shadow(b) runs beside extend(b + 1)
+// (they touch disjoint state) and shade(b + 1) waits for it, so each
+// launch's tail overlaps the other's work.
+struct WfSide {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t shaded = nullptr, shadowed = nullptr;
+};
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
                              cudaStream_t stream, StageTimer* timer = nullptr, const NrcWave* nrc = nullptr,
-                             gbrt_nrc* cache = nullptr);
+                             gbrt_nrc* cache = nullptr, const WfSide* side = nullptr);
 // Ray queries through the persistent world traversal (8-wide when built);
 // `work` is one device word used as the fetch cursor.
 cudaError_t launch_trace_rays_persistent(const DevScene& s, const gbrt_ray* rays, uint32_t n, uint32_t flags,

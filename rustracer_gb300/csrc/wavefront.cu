@@ -171,7 +171,11 @@ cudaError_t launch_resolve(const gbrt_ubo& ubo, const RenderOut& out, const floa
 }
 
 cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const RenderOut& out, const WfState& st,
-                             cudaStream_t stream, StageTimer* timer, const NrcWave* nrc, gbrt_nrc* cache) {
+                             cudaStream_t stream, StageTimer* timer, const NrcWave* nrc, gbrt_nrc* cache,
+                             const WfSide* side) {
+    // the overlap needs the stages' own events off and leaves the cache form serial
+    // (its apply step updates the radiance the shadow stage also updates)
+    if (timer || nrc) side = nullptr;
     if (ubo.number_of_bounces > kMaxBounces) return cudaErrorInvalidValue;
     cudaError_t e = grids(g_grid);
     if (e != cudaSuccess) return e;
@@ -224,6 +228,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 else if (mode == kTraceWideTlas) wf_extend<kTraceWideTlas><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
                 else wf_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
                 te();
+                if (side && b > 0 && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
                 tb(1);
                 if (nrc) wf_shade_nrc<<<g_grid.shade, 128, 0, stream>>>(w, st, b, *nrc);
                 else wf_shade<<<g_grid.shade, 128, 0, stream>>>(w, st, b);
@@ -237,11 +242,19 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                     te();
                 }
                 tb(2);
-                if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
-                else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
-                else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, stream>>>(w, st, b);
+                cudaStream_t ss = stream;
+                if (side) {
+                    if ((e = cudaEventRecord(side->shaded, stream)) != cudaSuccess) return e;
+                    if ((e = cudaStreamWaitEvent(side->stream, side->shaded, 0)) != cudaSuccess) return e;
+                    ss = side->stream;
+                }
+                if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+                else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+                else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+                if (side && (e = cudaEventRecord(side->shadowed, ss)) != cudaSuccess) return e;
                 te();
             }
+            if (side && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
             tb(3);
             if (nrc) wf_finish_nrc<<<(npw + 127) / 128, 128, 0, stream>>>(w, st, *nrc);
             else wf_finish<<<(npw + 127) / 128, 128, 0, stream>>>(w, st);
