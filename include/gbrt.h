@@ -424,7 +424,7 @@ int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices)
  * its render thread (record_raytracing_commands, crates/examples/
  * gltf_viewer/src/main.rs:244-270).  A job is one gbrt_render_ex call made
  * asynchronous.  Jobs on a context are traced by one scheduler thread on the
- * context's stream in waves of at most 2^21 paths; each wave packs segments
+ * context's stream in waves of at most 2^22 paths; each wave packs segments
  * (a pixel range x a sample range) of up to 32 admitted jobs, possibly of
  * different scenes, so jobs join and leave the running batch at wave
  * boundaries.  A job's image and accumulation are bit-identical to the same

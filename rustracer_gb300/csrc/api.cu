@@ -677,7 +677,7 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     uint32_t launches = 1;
     if (wave) {
         const uint64_t paths = (uint64_t)npix * ns;
-        const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
+        const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, kMaxWavePaths);
         CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
         const bool timed = opts && (opts->flags & GBRT_RENDER_STAGE_TIMING);
         CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, timed ? &c->timer : nullptr, nullptr, nullptr,

@@ -8,7 +8,7 @@
 //      its scene is skinned and rebuilt);
 //   2. packs one wave: active jobs ordered by the policy (shortest remaining
 //      paths first, or submission order) contribute segments -- k samples of
-//      a pixel chunk -- until the wave's 2^21 paths are used;
+//      a pixel chunk -- until the wave's kMaxWavePaths paths are used;
 //   3. launches it (wavefront.cu), and for every job whose last segment it
 //      carried, the job's resolve (accumulate + tone map);
 //   4. retires waves whose completion event has fired: finished jobs get
@@ -37,7 +37,9 @@ double now_ms() {
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-constexpr uint32_t kWaveCap = kMaxWavePaths;  // paths per wave
+// paths per batched wave: smaller than a single frame's waves so that a
+// wave, and the wait of a job that joins the batch, stays short
+constexpr uint32_t kWaveCap = kMaxWavePaths < (1u << 22) ? kMaxWavePaths : (1u << 22);
 constexpr uint32_t kChunkDiv = 8;             // pixel chunk = wave / 8 (finer packing)
 constexpr int kMaxInFlight = 2;
 
@@ -427,7 +429,7 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
     if (u.number_of_bounces > 31) return fail(c, GBRT_E_INVALID, "jobs trace at most 31 bounces");
     if (d->skins && d->nskin == 0) return fail(c, GBRT_E_INVALID, "skins given with nskin = 0");
     const uint64_t npix = (uint64_t)d->accum->w * d->accum->h;
-    if (npix > kWaveCap) return fail(c, GBRT_E_INVALID, "job image larger than 2^21 pixels");
+    if (npix > kWaveCap) return fail(c, GBRT_E_INVALID, "job image larger than " + std::to_string(kWaveCap) + " pixels");
     auto j = std::make_unique<Job>();
     j->scene = s;
     j->acc = d->accum;

@@ -23,10 +23,14 @@ struct RenderOut {
 // wavefront.cu: device buffers of the wavefront path tracer, `cap` paths.
 // Each job of a wave owns kWfCounters queue lengths and fetch cursors.
 constexpr int kWfCounters = 128;
-constexpr uint32_t kPidBits = 21;                    // path id bits of a queue entry
+#ifndef GBRT_PID_BITS
+#define GBRT_PID_BITS 26
+#endif
+constexpr uint32_t kPidBits = GBRT_PID_BITS;         // path id bits of a queue entry (segment: the rest)
+static_assert(kPidBits <= 26, "queue words keep at least 6 bits of segment index");
 constexpr uint32_t kMaxWavePaths = 1u << kPidBits;   // paths per wave
 constexpr int kMaxWaveJobs = 32;                     // jobs sharing one wave
-constexpr int kMaxWaveSegs = 256;                    // (pixel range x sample range) pieces per wave
+constexpr int kMaxWaveSegs = kPidBits <= 24 ? 256 : (1 << (32 - kPidBits));  // (pixels x samples) pieces per wave
 struct WfState {
     uint32_t cap;
     float4* ray_o[2];   // extension queues (ping-pong): origin

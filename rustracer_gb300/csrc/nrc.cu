@@ -671,7 +671,7 @@ extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, 
     const uint32_t W = acc->w, H = acc->h, ns = ubo->number_of_samples;
     const size_t npix = (size_t)W * H;
     const uint64_t paths = (uint64_t)npix * ns;
-    const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, 1u << 21);
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, kMaxWavePaths);
     CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
     const uint32_t tmax = std::max<uint32_t>(opts->train_samples, 1u) * 2u;  // room for the hash's spread
     if (r->f_cap < cap) {
