@@ -145,17 +145,18 @@ def common_line(args, n, value, ms_per_step, extra_cfg=None):
             "config": cfg}
 
 
-def traffic_from_profile(kernel):
-    """DRAM bytes (read + write) per launch of `kernel` at this workload, from
-    the committed ncu summary profiles/dram_traffic_icosphere7.json (null when
-    that kernel has no capture)."""
+def traffic_from_profile(kernel, rays_per_launch):
+    """DRAM bytes (read + write) per launch of `kernel`: the per-ray figure of
+    the committed ncu capture (profiles/dram_traffic_icosphere7.json, a
+    smaller case of this workload) times the rays of one launch here (null
+    when that kernel has no capture)."""
     p = os.path.join(ROOT, "profiles", "dram_traffic_icosphere7.json")
     if not os.path.exists(p):
         return None
     d = json.load(open(p)).get(kernel)
-    if not d or (d.get("width"), d.get("height"), d.get("spp")) != (W, H, SPP):
+    if not d or not rays_per_launch:
         return None
-    return d.get("dram_bytes_per_launch")
+    return d["dram_bytes_per_ray"] * rays_per_launch
 
 
 def run_gpu(args):
@@ -268,7 +269,11 @@ def run_gpu(args):
         stages = None
         kernel_name = "pt_megakernel"
         achieved = (rays * bray + shaded_t * B_SHADE) / (dev_ms / 1e3) / 1e9
-    traffic = traffic_from_profile(kernel_name)
+    max_wave = 1 << 26  # paths per single-frame wave (the library's kMaxWavePaths)
+    waves = -(-(W * H * SPP) // min(W * H * SPP, max_wave))
+    stage_launches = waves * DEPTH * stage_frames
+    rays_per_launch = (stage_rays[0] if kernel_name == "wf_extend" else stage_rays[2]) / max(stage_launches, 1)
+    traffic = traffic_from_profile(kernel_name, rays_per_launch)
     line = common_line(args, world, value, dev_ms / args.steps,
                        {"kernel": args.mode, "wall_ms_per_step": wall / args.steps * 1e3,
                         "launches_per_step": launches})
