@@ -174,11 +174,14 @@ def run_gpu(args):
     acc = gbrt.Accum(ctx, W, H)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
-    state = {"total": 0}
+    state = {"step": 0}
 
     def frame(out_ptr=None, timed=False):
-        state["total"] += SPP
-        ubo = np.asarray(sd.ubo(W, H, samples=SPP, total=state["total"], bounces=DEPTH, exposure=1.0)).reshape(())
+        # this rank's samples of the next step (disjoint across ranks)
+        from rustracer_gb300 import replicas
+        _, last = replicas.sample_range(rank, world, state["step"], SPP)
+        state["step"] += 1
+        ubo = np.asarray(sd.ubo(W, H, samples=SPP, total=last, bounces=DEPTH, exposure=1.0)).reshape(())
         st = np.zeros((), gbrt.T.STATS)
         opts = gbrt.RenderOpts(MODES[args.mode], 1 if timed else 0, None, None)  # 1 = per-stage CUDA events
         ctx.check(ctx.L.gbrt_render_ex(scene.h, gbrt._p(ubo), acc.h, out_ptr, gbrt._p(st), C.byref(opts)))
@@ -235,18 +238,9 @@ def run_gpu(args):
         e2e_s += time.perf_counter() - t
         e2e_rays += int(st["rays_total"])
 
-    stats = torch.tensor([dev_ms, wall, e2e_s, float(rays), float(e2e_rays)], dtype=torch.float64,
-                         device=f"cuda:{local}")
-    if world > 1:
-        import torch.distributed as dist
-        mx = stats.clone()
-        dist.all_reduce(mx[:3], op=dist.ReduceOp.MAX)
-        sm = stats.clone()
-        dist.all_reduce(sm[3:], op=dist.ReduceOp.SUM)
-        dev_ms, wall, e2e_s = (float(x) for x in mx[:3])
-        tot_rays, tot_e2e = float(sm[3]), float(sm[4])
-    else:
-        tot_rays, tot_e2e = float(rays), float(e2e_rays)
+    from rustracer_gb300 import replicas
+    (dev_ms, wall, e2e_s), (tot_rays, tot_e2e) = replicas.combine([dev_ms, wall, e2e_s], [rays, e2e_rays],
+                                                                  device=f"cuda:{local}")
     if rank != 0:
         return
     cs = cpu_sample(sd, target_s=args.cpu_seconds) if world == 1 else cpu_sample(sd, target_s=0.0)
