@@ -417,6 +417,20 @@ int gbrt_trace_rays_device(gbrt_scene* scene, const gbrt_ray* d_rays, uint32_t n
 #define GBRT_NOALLOC_MAX_TRIANGLES 65536u
 int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices);
 
+/* Autotuner (no reference counterpart; the reference leaves traversal to the
+ * driver).  Renders a probe frame (probe_ubo's camera, samples and bounces at
+ * width x height, into scratch memory) with the binary BVH and with the
+ * 8-wide BVH, three rounds each (the first warms up), and keeps the faster
+ * layout for this scene's later renders and jobs.  Synchronous. */
+typedef struct gbrt_tune_report {
+    double ms_binary;       /* best probe time, binary layout */
+    double ms_wide;         /* best probe time, 8-wide layout (0 if the scene has none) */
+    uint32_t chosen_width;  /* 2 or 8 */
+    uint32_t _pad;
+} gbrt_tune_report;
+int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t width, uint32_t height,
+                        gbrt_tune_report* report);
+
 /* ------------------------------------------------------------------------ */
 /* Jobs: asynchronous frames with continuous batching                       */
 /* ------------------------------------------------------------------------ */

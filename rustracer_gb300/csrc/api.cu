@@ -31,6 +31,7 @@ static_assert(sizeof(gbrt_skin_raw) == 16384, "Skin is 256 mat4");
 static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records");
 static_assert(sizeof(gbrt_stats) == 104, "stats record");
 static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 48, "job records");
+static_assert(sizeof(gbrt_tune_report) == 24, "tune report");
 
 namespace {
 thread_local std::string g_create_error;
@@ -708,6 +709,52 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
         CU(c, stage_timer_collect(c->timer, stats->stage_ms), "stage timing");
     if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit (status " +
                                                             std::to_string(dc.status) + ")");
+    return GBRT_OK;
+}
+
+int gbrt_scene_autotune(gbrt_scene* s, const gbrt_ubo* ubo, uint32_t width, uint32_t height, gbrt_tune_report* rep) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (!ubo || width == 0 || height == 0) return fail(c, GBRT_E_INVALID, "NULL probe UBO or empty probe image");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tuning");
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
+    if (ubo->number_of_bounces > 31 || ubo->number_of_samples == 0)
+        return fail(c, GBRT_E_INVALID, "probe needs 1..31 bounces and at least one sample");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t npix = (size_t)width * height;
+    const uint64_t paths = (uint64_t)npix * ubo->number_of_samples;
+    CU(c, wavefront_reserve(c, (uint32_t)std::min<uint64_t>(paths, kMaxWavePaths), npix), "cudaMalloc(wavefront)");
+    DevBuf probe;
+    CU(c, probe.alloc(npix * sizeof(float4)), "cudaMalloc(probe image)");
+    RenderOut out{};
+    out.width = width;
+    out.height = height;
+    out.accum = probe.as<float4>();
+    out.counters = c->counters.as<DeviceCounters>();
+    gbrt_ubo u = *ubo;
+    u.total_number_of_samples = u.number_of_samples;
+    double best[2] = {1e30, 1e30};  // [0] binary, [1] 8-wide
+    const bool has_wide = s->view.cw_nodes != nullptr || !s->view.has_world;
+    for (int rep_i = 0; rep_i < 3; ++rep_i)
+        for (int wide = 0; wide < (has_wide ? 2 : 1); ++wide) {
+            DevScene v = s->view;
+            v.prefer_binary = wide ? 0u : 1u;
+            CU(c, cudaEventRecord(c->ev0, st), "event");
+            CU(c, launch_wavefront(v, u, out, c->wf, st, nullptr, nullptr, nullptr, &c->side), "probe render");
+            CU(c, cudaEventRecord(c->ev1, st), "event");
+            CU(c, cudaStreamSynchronize(st), "sync");
+            float ms = 0.0f;
+            CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
+            if (rep_i > 0) best[wide] = std::min(best[wide], (double)ms);  // the first round warms up
+        }
+    s->view.prefer_binary = (!has_wide || best[0] < best[1]) ? 1u : 0u;
+    if (rep) {
+        rep->ms_binary = best[0];
+        rep->ms_wide = has_wide ? best[1] : 0.0;
+        rep->chosen_width = s->view.prefer_binary ? 2u : 8u;
+        rep->_pad = 0;
+    }
     return GBRT_OK;
 }
 

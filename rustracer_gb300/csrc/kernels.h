@@ -82,7 +82,13 @@ struct WaveRing {
     WaveDesc* host = nullptr;
     cudaEvent_t ev[kSlots] = {};
     int next = 0;
+    // captured launch sequences of batched waves, per traversal form and
+    // bounce count, valid for the wavefront buffers in graph_state
+    cudaGraphExec_t graph[3][32] = {};
+    WfState graph_state{};
 };
+// Drops the captured graphs (the ring's buffers stay).
+void wave_graphs_reset(WaveRing& r);
 cudaError_t wave_ring_init(WaveRing& r);
 void wave_ring_free(WaveRing& r);
 // Waits until the next slot is free and returns it for filling.

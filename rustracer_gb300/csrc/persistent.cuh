@@ -297,10 +297,10 @@ GB_D void world_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t fl
 }
 
 // The form a scene needs: binary when it has a world BVH without its
-// 8-wide copy (after gbrt_scene_rebuild_noalloc), else 8-wide, with the TLAS
-// when it has transformed instances.
+// 8-wide copy (after gbrt_scene_rebuild_noalloc) or when the autotuner chose
+// it, else 8-wide, with the TLAS when it has transformed instances.
 inline int trace_mode(const DevScene& s) {
-    if (s.has_world && !s.cw_nodes) return kTraceBinary;
+    if (s.prefer_binary || (s.has_world && !s.cw_nodes)) return kTraceBinary;
     return s.has_tlas ? kTraceWideTlas : kTraceWide;
 }
 

@@ -105,6 +105,7 @@ struct DevScene {
     const uchar4* sky;   // 6 faces, size^2 each
     uint32_t sky_size;
     uint32_t all_opaque; // every geometry is OPAQUE: the any-hit test never runs
+    uint32_t prefer_binary;  // autotuner's choice: traverse the binary layout even where 8-wide nodes exist
 };
 
 }  // namespace gbrt

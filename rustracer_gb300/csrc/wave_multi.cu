@@ -7,6 +7,9 @@
 // serves one job and reads its scene and UBO with uniform constant loads.
 // The job queue (jobs.cu) packs the waves; the kernel bodies are the
 // single-frame ones (wavefront.cuh).
+#include <algorithm>
+#include <cstring>
+
 #include "wavefront.cuh"
 
 namespace gbrt {
@@ -49,7 +52,12 @@ struct MultiWave {
 
 }  // namespace
 
-__global__ void __launch_bounds__(128) wfm_camera(WfState st) { camera_body(MultiWave{}, st); }
+// camera and finish loop over the wave with a fixed grid, so that one
+// captured graph serves every wave of the same bounce count
+__global__ void __launch_bounds__(128) wfm_camera(WfState st) {
+    for (uint32_t base = blockIdx.x * blockDim.x; base < c_wave.npaths; base += gridDim.x * blockDim.x)
+        camera_body(MultiWave{}, st, base + threadIdx.x);
+}
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_extend(WfState st, uint32_t b) {
     extend_body<kMode>(MultiWave{}, st, b);
@@ -59,7 +67,10 @@ template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_shadow(WfState st, uint32_t b) {
     shadow_body<kMode>(MultiWave{}, st, b);
 }
-__global__ void __launch_bounds__(128) wfm_finish(WfState st) { finish_body(MultiWave{}, st); }
+__global__ void __launch_bounds__(128) wfm_finish(WfState st) {
+    for (uint32_t base = blockIdx.x * blockDim.x; base < c_wave.nfin; base += gridDim.x * blockDim.x)
+        finish_body(MultiWave{}, st, base + threadIdx.x);
+}
 
 // --- host side ---------------------------------------------------------------
 cudaError_t init_wave_multi_constants(const float* srgb_lut) {
@@ -109,6 +120,7 @@ cudaError_t wave_ring_init(WaveRing& r) {
 }
 
 void wave_ring_free(WaveRing& r) {
+    wave_graphs_reset(r);
     for (int i = 0; i < WaveRing::kSlots; ++i) {
         if (r.ev[i]) {
             cudaEventSynchronize(r.ev[i]);
@@ -131,37 +143,46 @@ cudaError_t wave_acquire(WaveRing& r, WaveDesc** slot) {
 cudaError_t wave_partition(WaveDesc& w) {
     cudaError_t e = grids(g_grid);
     if (e != cudaSuccess) return e;
+    // exactly the stage's full grid, in proportion to each job's paths (at
+    // least one block each), so that the launches of every wave are alike
     const int full[3] = {g_grid.extend, g_grid.shade, g_grid.shadow};
     for (int k = 0; k < 3; ++k) {
+        const uint32_t total = std::max<uint32_t>((uint32_t)full[k], w.njobs);
+        uint32_t n[kMaxWaveJobs], sum = 0, big = 0;
+        for (uint32_t j = 0; j < w.njobs; ++j) {
+            const uint64_t share = (uint64_t)total * w.jobs[j].npaths / (w.npaths ? w.npaths : 1);
+            n[j] = share > 0 ? (uint32_t)share : 1u;
+            sum += n[j];
+            if (n[j] > n[big]) big = j;
+        }
+        n[big] = n[big] + total - sum;  // the remainder (either sign) to the largest job
         uint32_t acc = 0;
         for (uint32_t j = 0; j < w.njobs; ++j) {
             w.blk[k][j] = acc;
-            const uint64_t share = ((uint64_t)full[k] * w.jobs[j].npaths + w.npaths / 2) / (w.npaths ? w.npaths : 1);
-            acc += share > 0 ? (uint32_t)share : 1u;
+            acc += n[j];
         }
         w.blk[k][w.njobs] = acc;
     }
     return cudaSuccess;
 }
 
-cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, StageTimer* timer) {
-    const WaveDesc& w = ring.host[ring.next];
-    if (w.nb > kMaxBounces || w.njobs == 0 || w.njobs > kMaxWaveJobs || w.nsegs == 0 || w.nsegs > kMaxWaveSegs ||
-        w.npaths > st.cap || w.npaths > kMaxWavePaths)
-        return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_wave, &w, sizeof(WaveDesc), 0, cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaEventRecord(ring.ev[ring.next], stream)) != cudaSuccess) return e;
-    ring.next = (ring.next + 1) % WaveRing::kSlots;
-    if ((e = cudaMemsetAsync(st.counts, 0, (size_t)w.njobs * kWfCounters * sizeof(uint32_t), stream)) != cudaSuccess)
-        return e;
+namespace {
+
+int wave_mode(const WaveDesc& w) {
     int mode = kTraceWide;  // the most general form any job's scene needs
     for (uint32_t j = 0; j < w.njobs; ++j) {
         const int m = trace_mode(w.jobs[j].s);
         if (m == kTraceBinary) mode = kTraceBinary;
         else if (m == kTraceWideTlas && mode == kTraceWide) mode = kTraceWideTlas;
     }
-    if (timer && (e = stage_timer_reserve(*timer, timer->used + 2 + 3 * (int)w.nb + 1)) != cudaSuccess) return e;
+    return mode;
+}
+
+// The launches of one batched wave with `nb` bounces in traversal form
+// `mode`; every grid is fixed, the wave itself is read from c_wave.
+cudaError_t enqueue_wave(const WfState& st, int mode, uint32_t nb, cudaStream_t stream, StageTimer* timer) {
+    cudaError_t e = cudaMemsetAsync(st.counts, 0, (size_t)kMaxWaveJobs * kWfCounters * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
     auto tb = [&](int stage) {
         if (timer) {
             timer->stage[timer->used] = stage;
@@ -171,28 +192,81 @@ cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, 
     auto te = [&]() {
         if (timer) cudaEventRecord(timer->ev[2 * timer->used++ + 1], stream);
     };
+    const int flat = 4 * g_grid.shade;  // grid-stride kernels
     tb(3);
-    wfm_camera<<<(w.npaths + 127) / 128, 128, 0, stream>>>(st);
+    wfm_camera<<<flat, 128, 0, stream>>>(st);
     te();
-    for (uint32_t b = 0; b < w.nb; ++b) {
+    for (uint32_t b = 0; b < nb; ++b) {
         tb(0);
-        if (mode == kTraceWide) wfm_extend<kTraceWide><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
-        else if (mode == kTraceWideTlas) wfm_extend<kTraceWideTlas><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
-        else wfm_extend<kTraceBinary><<<w.blk[0][w.njobs], 128, 0, stream>>>(st, b);
+        if (mode == kTraceWide) wfm_extend<kTraceWide><<<g_grid.extend, 128, 0, stream>>>(st, b);
+        else if (mode == kTraceWideTlas) wfm_extend<kTraceWideTlas><<<g_grid.extend, 128, 0, stream>>>(st, b);
+        else wfm_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(st, b);
         te();
         tb(1);
-        wfm_shade<<<w.blk[1][w.njobs], 128, 0, stream>>>(st, b);
+        wfm_shade<<<g_grid.shade, 128, 0, stream>>>(st, b);
         te();
         tb(2);
-        if (mode == kTraceWide) wfm_shadow<kTraceWide><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
-        else if (mode == kTraceWideTlas) wfm_shadow<kTraceWideTlas><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
-        else wfm_shadow<kTraceBinary><<<w.blk[2][w.njobs], 128, 0, stream>>>(st, b);
+        if (mode == kTraceWide) wfm_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(st, b);
+        else if (mode == kTraceWideTlas) wfm_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, stream>>>(st, b);
+        else wfm_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, stream>>>(st, b);
         te();
     }
     tb(3);
-    wfm_finish<<<(w.nfin + 127) / 128, 128, 0, stream>>>(st);
+    wfm_finish<<<flat, 128, 0, stream>>>(st);
     te();
     return cudaGetLastError();
+}
+
+}  // namespace
+
+void wave_graphs_reset(WaveRing& r) {
+    for (auto& row : r.graph)
+        for (auto& g : row)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    r.graph_state = WfState{};
+}
+
+cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, StageTimer* timer) {
+    const WaveDesc& w = ring.host[ring.next];
+    if (w.nb > kMaxBounces || w.njobs == 0 || w.njobs > kMaxWaveJobs || w.nsegs == 0 || w.nsegs > kMaxWaveSegs ||
+        w.npaths > st.cap || w.npaths > kMaxWavePaths)
+        return cudaErrorInvalidValue;
+    for (int k = 0; k < 3; ++k)
+        if (w.blk[k][w.njobs] != (uint32_t)(k == 0 ? g_grid.extend : k == 1 ? g_grid.shade : g_grid.shadow))
+            return cudaErrorInvalidValue;  // wave_partition fills the grids these launches use
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_wave, &w, sizeof(WaveDesc), 0, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ring.ev[ring.next], stream)) != cudaSuccess) return e;
+    ring.next = (ring.next + 1) % WaveRing::kSlots;
+    const int mode = wave_mode(w);
+    if (timer) {
+        if ((e = stage_timer_reserve(*timer, timer->used + 2 + 3 * (int)w.nb + 1)) != cudaSuccess) return e;
+        return enqueue_wave(st, mode, w.nb, stream, timer);
+    }
+    // one CUDA graph per (traversal form, bounce count), captured on first use
+    // and replayed for every later wave; rebuilt when the wavefront buffers move
+    if (std::memcmp(&ring.graph_state, &st, sizeof(WfState)) != 0) {
+        wave_graphs_reset(ring);
+        ring.graph_state = st;
+    }
+    cudaGraphExec_t& exec = ring.graph[mode][w.nb];
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+        const cudaError_t ee = enqueue_wave(st, mode, w.nb, stream, nullptr);
+        e = cudaStreamEndCapture(stream, &graph);
+        if (ee != cudaSuccess) e = ee;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            exec = nullptr;
+            return e;
+        }
+    }
+    return cudaGraphLaunch(exec, stream);
 }
 
 }  // namespace gbrt

@@ -35,7 +35,7 @@ struct SingleWave {
 }  // namespace
 
 __global__ void __launch_bounds__(128) wf_camera(const __grid_constant__ SingleWave w, WfState st) {
-    camera_body(w, st);
+    camera_body(w, st, blockIdx.x * blockDim.x + threadIdx.x);
 }
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode))
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
     shadow_body<kMode>(w, st, b);
 }
 __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleWave w, WfState st) {
-    finish_body(w, st);
+    finish_body(w, st, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Radiance-cache forms of shade and finish, and the step that adds
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(128) wf_shade_nrc(const __grid_constant__ Sing
 }
 __global__ void __launch_bounds__(128) wf_finish_nrc(const __grid_constant__ SingleWave w, WfState st,
                                                      const __grid_constant__ NrcWave nrc) {
-    finish_body<SingleWave, true>(w, st, &nrc);
+    finish_body<SingleWave, true>(w, st, blockIdx.x * blockDim.x + threadIdx.x, &nrc);
 }
 __global__ void __launch_bounds__(256) wf_nrc_apply(WfState st, NrcWave nrc, uint32_t b) {
     const uint32_t n = nrc.counts[b];

@@ -95,8 +95,7 @@ GB_D void flush_trace_stats(const TraceStats& ts, DeviceCounters* c) {
 // rgen:32-80 for every path of the wave: seeds (D1), camera ray, path state.
 // Job j's first queue is its paths in order, at the paths' own positions.
 template <class Wv>
-GB_D void camera_body(const Wv& w, const WfState& st) {
-    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+GB_D void camera_body(const Wv& w, const WfState& st, uint32_t pid) {
     if (pid >= w.npaths()) return;
     const uint32_t si = w.seg_of_path(pid);
     const WaveSeg& sg = w.seg(si);
@@ -345,8 +344,7 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b) {
 // Per pixel of every segment: add its samples' radiance to the job's frame
 // sum in sample order (the megakernel's per-pixel order), keep the last Ray.t.
 template <class Wv, bool kNrc = false>
-GB_D void finish_body(const Wv& w, const WfState& st, const NrcWave* nrc = nullptr) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave* nrc = nullptr) {
     if (i >= w.nfin()) return;
     const WaveSeg& sg = w.seg(w.seg_of_fin(i));
     const WaveJob& J = w.job(sg.job);

@@ -67,6 +67,7 @@ SIGNATURES = {
     "gbrt_nrc_query": (i32, [P, P, u32, P]),
     "gbrt_nrc_train": (i32, [P, P, P, u32, i32, P, P, P]),
     "gbrt_render_nrc": (i32, [P, P, P, P, P, P, P, P]),
+    "gbrt_scene_autotune": (i32, [P, P, u32, u32, P]),
 }
 JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
 POLICY_SRPT, POLICY_FIFO = 0, 1
@@ -358,6 +359,14 @@ class Scene:
     def set_skybox(self, size, faces):
         faces = None if faces is None else np.ascontiguousarray(faces, np.uint8)
         self.ctx.check(self.ctx.L.gbrt_skybox_set(self.h, size, _p(faces)))
+
+    def autotune(self, ubo, width, height):
+        """gbrt_scene_autotune: picks the faster BVH layout; returns
+        dict(ms_binary, ms_wide, chosen_width)."""
+        rep = np.zeros(3, np.float64)
+        ubo = np.asarray(ubo, T.UBO).reshape(())
+        self.ctx.check(self.ctx.L.gbrt_scene_autotune(self.h, _p(ubo), width, height, _p(rep)))
+        return dict(ms_binary=float(rep[0]), ms_wide=float(rep[1]), chosen_width=int(rep[2:].view(np.uint32)[0]))
 
     def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False):
         """One frame (record_raytracing_commands + the shaders).  Returns a dict
