@@ -225,12 +225,16 @@ int build_all(gbrt_scene* s) {
         CU(c, s->cw_tris.alloc(nw * sizeof(TriRec)), "cudaMalloc(wide triangles)");
         CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
                                    s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)nw,
-                                   s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), &s->cw_count, st),
+                                   s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), &s->cw_count, st,
+                                   &s->cw_levels),
            "build wide world BVH");
+        s->nworld = (uint32_t)nw;
     } else {
         s->cw_nodes.release();
         s->cw_tris.release();
         s->cw_count = 0;
+        s->cw_levels.clear();
+        s->nworld = 0;
     }
     // BLASes + TLAS
     if (!tlas_ids.empty()) {
@@ -339,7 +343,33 @@ int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin) {
     CU(c, launch_skinning(s->base_vertices.as<gbrt_vertex>(), s->vertices.as<gbrt_vertex>(), s->nv,
                           s->skins.as<gbrt_skin_raw>(), nskin, st),
        "skinning");
-    return build_all(s);
+    return refit_world(s);
+}
+
+int refit_world(gbrt_scene* s) {
+    gbrt_ctx* c = s->ctx;
+    DevScene& v = s->view;
+    // transformed instances (BLAS boxes feed the TLAS) or no 8-wide copy: full rebuild
+    if (v.has_tlas || !v.has_world || !s->cw_count || s->cw_levels.size() < 2) return build_all(s);
+    cudaStream_t st = c->stream;
+    // binary world BVH: rebuilt (an LBVH over the same items, one launch chain);
+    // 8-wide world BVH: refit in place, keeping its topology and slots
+    BvhResult r;
+    CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
+                             s->items.as<uint4>(), s->nworld, s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r,
+                             st),
+       "rebuild world BVH");
+    CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4)), "cudaMalloc(refit boxes)");
+    CU(c, refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
+                               s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), s->nworld, s->cw_levels,
+                               s->cw_boxes.as<float4>(), st),
+       "refit wide world BVH");
+    CU(c, cudaStreamSynchronize(st), "sync after refit");
+    v.world_root = r.root;
+    v.world_lo = r.lo;
+    v.world_hi = r.hi;
+    refresh_view(s);
+    return GBRT_OK;
 }
 
 }  // namespace gbrt_host

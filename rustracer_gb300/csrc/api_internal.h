@@ -85,6 +85,9 @@ struct gbrt_scene {
     gbrt_host::DevBuf nodes, tris, inst, items;
     gbrt_host::DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
     gbrt_host::DevBuf blas_cw_nodes, blas_cw_tris;  // 8-wide BLASes of transformed instances
+    std::vector<uint32_t> cw_levels;  // first node of each level of the 8-wide world BVH (for refit)
+    gbrt_host::DevBuf cw_boxes;        // refit scratch: float boxes of the 8-wide nodes
+    uint32_t nworld = 0;               // triangles in the world BVH
     uint32_t cw_count = 0;
     bool built = false;
     std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene
@@ -128,9 +131,13 @@ struct DeviceGuard {
 cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix);
 // Rebuilds the world BVH, BLASes and TLAS of a scene from its current vertices.
 int build_all(gbrt_scene* s);
-// Linear-blend skinning of the scene's bind-pose vertices, then build_all.
+// Linear-blend skinning of the scene's bind-pose vertices, then refit_world.
 int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin);
 void fill_stats(gbrt_stats* st, const DeviceCounters& dc, double ms, uint32_t launches);
+// After the vertices moved: the binary world BVH rebuilt and the 8-wide one
+// refit in place (topology kept); scenes with transformed instances rebuild
+// everything (build_all).
+int refit_world(gbrt_scene* s);
 
 // nrc.cu: cache queries and one training step on device arrays (stream-ordered).
 cudaError_t nrc_query_device(gbrt_nrc* r, const float4* q, uint32_t n, float4* out, cudaStream_t st);

@@ -1,6 +1,7 @@
 // kernels.h — host-visible launchers of the device code.
 #pragma once
 #include <cuda_runtime.h>
+#include <vector>
 #include "scene.cuh"
 
 namespace gbrt {
@@ -212,7 +213,15 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_v
 // the node count.
 cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  const uint4* items, uint32_t n, CwNode* nodes, TriRec* tris, uint32_t* nodes_used,
-                                 cudaStream_t st);
+                                 cudaStream_t st, std::vector<uint32_t>* level_starts = nullptr);
+// Refit of an 8-wide BVH built by build_triangle_cwbvh over the same
+// triangles: triangle records re-read from the vertices, then every node's
+// grid and child boxes recomputed level by level (level_starts: first node
+// of each level, last entry = node count).  boxes: 2 float4 per node scratch.
+// No host synchronisation.
+cudaError_t refit_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
+                                 CwNode* nodes, TriRec* tris, uint32_t ntris, const std::vector<uint32_t>& level_starts,
+                                 float4* boxes, cudaStream_t st);
 
 // TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
 // the instance ids.
