@@ -312,7 +312,18 @@ int gbrt_scene_destroy(gbrt_scene* scene);
 
 /* Builds one BLAS per geometry range on the GPU (Morton LBVH).  Replaces the
  * per-primitive vkCmdBuildAccelerationStructuresKHR of create_as
- * (acceleration_structures.rs:17-76,79-111).  flags: reserved, 0. */
+ * (acceleration_structures.rs:17-76,79-111).
+ *
+ * flags: 0, or GBRT_BUILD_NO_FLATTEN.  By default the next gbrt_tlas_build
+ * flattens transformed instances into the world BVH when the flattened scene
+ * has at most GBRT_FLATTEN_MAX_TRIANGLES triangles: their triangles are
+ * transformed to world space once (row-major 3x4, each product and sum
+ * rounded on its own) and intersected there, so every ray walks one 8-wide
+ * BVH.  GBRT_BUILD_NO_FLATTEN keeps them in BLASes under a TLAS, where rays
+ * are transformed to object space instead.  The two give hits that can
+ * differ in the last bits of t, u, v (the oracle follows the same rule). */
+#define GBRT_BUILD_NO_FLATTEN 0x1u
+#define GBRT_FLATTEN_MAX_TRIANGLES (1u << 26)
 int gbrt_blas_build(gbrt_scene* scene, const gbrt_geo_range* ranges, uint32_t n,
                     uint32_t flags);
 

@@ -600,6 +600,7 @@ struct BNode {
 struct Bvh {
     std::vector<BNode> nodes;
     std::vector<uint32_t> refs;  // leaf order -> primitive reference
+    std::vector<float> pos;      // world BVH: 9 floats (3 vertices) per primitive reference
 };
 
 // Binned SAH BVH2 (16 bins, leaf <= 4 refs, traversal cost 1, test cost 1).
@@ -733,7 +734,9 @@ struct orc_scene {
     std::vector<char> blas_needed;
     // TLAS
     std::vector<Instance> inst;
-    Bvh world;                           // merged BVH over identity-instance triangles
+    Bvh world;                           // merged BVH over identity-instance (and flattened) triangles
+    uint32_t build_flags = 0;            // GBRT_BUILD_NO_FLATTEN
+    bool flattened = false;
     std::vector<uint64_t> world_refs;    // (instance << 32) | prim
     Bvh tlas;                            // over entries: 0 = world (if any), then instances
     std::vector<int32_t> tlas_entries;   // -1 = world BVH, else instance index
@@ -884,9 +887,16 @@ bool traverse_bvh(const orc_scene& s, const Bvh& bvh, const TRay<T>& r, T tmin, 
         if (n.count > 0) {
             for (int i = 0; i < n.count; ++i) {
                 uint32_t inst, prim, bgeo, geo;
-                resolve(bvh.refs[n.first + i], inst, prim, bgeo, geo);
+                const uint32_t ref = bvh.refs[n.first + i];
+                resolve(ref, inst, prim, bgeo, geo);
                 const float *p0, *p1, *p2;
-                tri_vertices(s, bgeo, prim, p0, p1, p2);
+                if (!bvh.pos.empty()) {  // stored (world-space) triangle
+                    p0 = &bvh.pos[9 * (size_t)ref];
+                    p1 = p0 + 3;
+                    p2 = p0 + 6;
+                } else {
+                    tri_vertices(s, bgeo, prim, p0, p1, p2);
+                }
                 cnt.tris++;
                 T t;
                 float u, v;
@@ -1481,30 +1491,50 @@ void rebuild(orc_scene& s) {
         }
         build_bvh(boxes, s.blas[g]);
     }
-    // merged world BVH over identity instances
+    // merged world BVH over identity instances, and over transformed ones too
+    // when the flattened scene has at most GBRT_FLATTEN_MAX_TRIANGLES
+    // triangles (their vertices transformed once, mul34 unfused), unless the
+    // build asked for GBRT_BUILD_NO_FLATTEN -- the rule of the library's build
+    uint64_t flat_total = 0;
+    for (size_t i = 0; i < s.inst.size(); ++i)
+        if ((s.inst[i].mask & 0xFFu) != 0) flat_total += s.ranges[s.inst[i].blas].i_len / 3;
+    s.flattened = !(s.build_flags & GBRT_BUILD_NO_FLATTEN) && flat_total <= GBRT_FLATTEN_MAX_TRIANGLES;
     s.world_refs.clear();
     std::vector<Aabb> wboxes;
+    std::vector<float> wpos;
     for (size_t i = 0; i < s.inst.size(); ++i) {
-        if (!s.inst[i].identity) continue;
-        uint32_t g = s.inst[i].blas;
+        const Instance& in = s.inst[i];
+        if (!in.identity && !(s.flattened && (in.mask & 0xFFu) != 0)) continue;
+        uint32_t g = in.blas;
         uint32_t ntri = s.ranges[g].i_len / 3;
         for (uint32_t p = 0; p < ntri; ++p) {
-            const float *p0, *p1, *p2;
-            tri_vertices(s, g, p, p0, p1, p2);
+            const float* pv[3];
+            tri_vertices(s, g, p, pv[0], pv[1], pv[2]);
             Aabb b;
-            b.grow(p0); b.grow(p1); b.grow(p2);
+            for (int k = 0; k < 3; ++k) {
+                float q[3] = {pv[k][0], pv[k][1], pv[k][2]};
+                if (!in.identity) {
+                    vec3 w = mul34(in.xf, vec4(q[0], q[1], q[2], 1.0f));
+                    q[0] = w.x;
+                    q[1] = w.y;
+                    q[2] = w.z;
+                }
+                b.grow(q);
+                wpos.insert(wpos.end(), q, q + 3);
+            }
             wboxes.push_back(b);
             s.world_refs.push_back(((uint64_t)i << 32) | p);
         }
     }
     s.world = Bvh();
     if (!wboxes.empty()) build_bvh(wboxes, s.world);
+    s.world.pos = std::move(wpos);
     // TLAS entries
     s.tlas_entries.clear();
     std::vector<Aabb> tboxes;
     if (!s.world.nodes.empty()) { s.tlas_entries.push_back(-1); tboxes.push_back(s.world.nodes[0].box); }
     for (size_t i = 0; i < s.inst.size(); ++i) {
-        if (s.inst[i].identity) continue;
+        if (s.inst[i].identity || s.flattened) continue;
         const Bvh& b = s.blas[s.inst[i].blas];
         if (b.nodes.empty()) continue;
         Aabb ob = b.nodes[0].box, wb;
@@ -1578,6 +1608,11 @@ int orc_blas_build(orc_scene* s, const gbrt_geo_range* r, uint32_t n) {
         s->ranges[r[i].geo_id] = r[i];
         s->geo_opaque[r[i].geo_id] = r[i].opaque ? 1 : 0;
     }
+    return GBRT_OK;
+}
+
+int orc_build_flags(orc_scene* s, uint32_t flags) {
+    s->build_flags = flags;
     return GBRT_OK;
 }
 

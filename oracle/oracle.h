@@ -38,6 +38,8 @@ orc_scene* orc_scene_create(const gbrt_vertex* v, uint32_t nv, const uint32_t* i
 void orc_scene_destroy(orc_scene* s);
 int  orc_blas_build(orc_scene* s, const gbrt_geo_range* ranges, uint32_t n);
 int  orc_tlas_build(orc_scene* s, const gbrt_instance* inst, uint32_t n);
+/* GBRT_BUILD_NO_FLATTEN keeps transformed instances in BLASes (set before orc_tlas_build). */
+int  orc_build_flags(orc_scene* s, uint32_t flags);
 int  orc_lights_set(orc_scene* s, const gbrt_light_raw* d, uint32_t nd,
                     const gbrt_light_raw* p, uint32_t np);
 int  orc_skybox_set(orc_scene* s, uint32_t face_size, const uint8_t* rgba8_faces);

@@ -35,6 +35,7 @@ def lib():
         L.orc_scene_destroy.argtypes = [P]
         L.orc_blas_build.argtypes = [P, P, u32]
         L.orc_tlas_build.argtypes = [P, P, u32]
+        L.orc_build_flags.argtypes = [P, u32]
         L.orc_lights_set.argtypes = [P, P, u32, P, u32]
         L.orc_skybox_set.argtypes = [P, u32, P]
         L.orc_skin.argtypes = [P, P, u32]
@@ -86,7 +87,7 @@ def tex_descs(textures):
 class OracleScene:
     """The oracle's copy of a SceneData, with its BLAS/TLAS built."""
 
-    def __init__(self, sd):
+    def __init__(self, sd, build_flags=0):
         L = lib()
         self.sd = sd
         descs, keep = tex_descs(sd.textures)
@@ -94,6 +95,7 @@ class OracleScene:
                                     _p(sd.prims), len(sd.prims), _p(sd.materials), len(sd.materials),
                                     C.cast(descs, C.c_void_p), len(sd.textures))
         assert L.orc_blas_build(self.h, _p(sd.geo_ranges), len(sd.geo_ranges)) == 0
+        assert L.orc_build_flags(self.h, build_flags) == 0
         assert L.orc_tlas_build(self.h, _p(sd.instances), len(sd.instances)) == 0
         assert L.orc_lights_set(self.h, _p(sd.dlights), len(sd.dlights), _p(sd.plights), len(sd.plights)) == 0
         if sd.skybox is not None:

@@ -153,6 +153,16 @@ int build_all(gbrt_scene* s) {
     std::vector<uint32_t> tlas_ids;
     std::vector<uint8_t> blas_needed(s->ngeo, 0);
     bool all_opaque = true;
+    // flatten transformed instances into the world BVH when the flattened
+    // scene stays within GBRT_FLATTEN_MAX_TRIANGLES (and the build allows it)
+    uint64_t flat_total = 0;
+    for (size_t i = 0; i < ninst; ++i) {
+        const gbrt_instance& in = s->instances[i];
+        const uint32_t g = (uint32_t)in.blas_handle;
+        if ((in.custom_index_and_mask >> 24) == 0 || g >= s->ngeo || !s->has_range[g]) continue;
+        flat_total += s->ranges[g].i_len / 3;
+    }
+    const bool flatten = !(s->build_flags & GBRT_BUILD_NO_FLATTEN) && flat_total <= GBRT_FLATTEN_MAX_TRIANGLES;
     for (size_t i = 0; i < ninst; ++i) {
         const gbrt_instance& in = s->instances[i];
         DevInstance& d = hinst[i];
@@ -176,7 +186,7 @@ int build_all(gbrt_scene* s) {
         d.identity = is_identity(in.transform) && (d.mask & 0xFFu) != 0;
         if ((d.mask & 0xFFu) == 0 || ntri == 0) continue;
         if (!r.opaque) all_opaque = false;
-        if (d.identity) {
+        if (d.identity || flatten) {
             for (uint32_t p = 0; p < ntri; ++p)
                 world_items.push_back(make_uint4((uint32_t)i, d.blas_geo, p, r.opaque ? 1u : 0u));
         } else {
@@ -208,13 +218,17 @@ int build_all(gbrt_scene* s) {
     v.has_tlas = 0;
     v.all_opaque = all_opaque ? 1u : 0u;
     s->all_opaque = all_opaque;
+    // instances first: the world build transforms the triangles of flattened ones
+    CU(c, upload(s->inst, hinst.data(), hinst.size(), st), "upload(instances)");
+    if (hinst.empty()) CU(c, s->inst.alloc(sizeof(DevInstance)), "cudaMalloc");
     // world BVH
     if (!world_items.empty()) {
         CU(c, upload(s->items, world_items.data(), world_items.size(), st), "upload(items)");
         BvhResult r;
         CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
                                  s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)world_items.size(),
-                                 s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st),
+                                 s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st,
+                                 s->inst.as<DevInstance>()),
            "build world BVH");
         v.has_world = 1;
         v.world_root = r.root;
@@ -226,7 +240,7 @@ int build_all(gbrt_scene* s) {
         CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
                                    s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)nw,
                                    s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), &s->cw_count, st,
-                                   &s->cw_levels),
+                                   &s->cw_levels, s->inst.as<DevInstance>()),
            "build wide world BVH");
         s->nworld = (uint32_t)nw;
     } else {
@@ -305,8 +319,6 @@ int build_all(gbrt_scene* s) {
     } else {
         s->blas_cw_nodes.release();
         s->blas_cw_tris.release();
-        CU(c, upload(s->inst, hinst.data(), std::max<size_t>(hinst.size(), 0), st), "upload(instances)");
-        if (hinst.empty()) CU(c, s->inst.alloc(sizeof(DevInstance)), "cudaMalloc");
         CU(c, cudaStreamSynchronize(st), "sync after build");
     }
     refresh_view(s);
@@ -357,12 +369,12 @@ int refit_world(gbrt_scene* s) {
     BvhResult r;
     CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
                              s->items.as<uint4>(), s->nworld, s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r,
-                             st),
+                             st, s->inst.as<DevInstance>()),
        "rebuild world BVH");
     CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4)), "cudaMalloc(refit boxes)");
     CU(c, refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
                                s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), s->nworld, s->cw_levels,
-                               s->cw_boxes.as<float4>(), st),
+                               s->cw_boxes.as<float4>(), st, s->inst.as<DevInstance>()),
        "refit wide world BVH");
     CU(c, cudaStreamSynchronize(st), "sync after refit");
     v.world_root = r.root;
@@ -547,7 +559,8 @@ int gbrt_blas_build(gbrt_scene* s, const gbrt_geo_range* r, uint32_t n, uint32_t
     gbrt_ctx* c = s->ctx;
     if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && !r) return fail(c, GBRT_E_INVALID, "ranges is NULL");
-    if (flags != 0) return fail(c, GBRT_E_INVALID, "flags must be 0");
+    if (flags & ~GBRT_BUILD_NO_FLATTEN) return fail(c, GBRT_E_INVALID, "unknown build flags");
+    s->build_flags = flags;
     for (uint32_t i = 0; i < n; ++i) {
         const gbrt_geo_range& g = r[i];
         if (g.geo_id >= s->ngeo) return fail(c, GBRT_E_INVALID, "geo_id out of range");
@@ -927,7 +940,10 @@ extern "C" int gbrt_scene_rebuild_noalloc(gbrt_scene* s, const gbrt_vertex* d_ve
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS with gbrt_tlas_build before rebuilding");
-    if (s->view.has_tlas)
+    bool transformed = s->view.has_tlas;  // flattened transformed instances have no TLAS but count too
+    for (const gbrt_instance& in : s->instances)
+        transformed = transformed || ((in.custom_index_and_mask >> 24) != 0 && !is_identity(in.transform));
+    if (transformed)
         return fail(c, GBRT_E_INVALID,
                     "the allocation-free rebuild covers scenes whose instances all have identity transforms");
     if (!s->view.has_world) return fail(c, GBRT_E_NOT_BUILT, "the scene has no world BVH");

@@ -59,8 +59,11 @@ struct Scratch {
     size_t cub_bytes;
 };
 
+// Item i's triangle (world space when `inst` is given and the item's
+// instance is a flattened transformed one), its box and TriRec.
 __global__ void tri_boxes_kernel(const gbrt_vertex* V, const uint32_t* I, const gbrt_priminfo* P, const uint4* items,
-                                 uint32_t n, float4* lo, float4* hi, TriRec* unsorted, uint32_t* cb) {
+                                 uint32_t n, float4* lo, float4* hi, TriRec* unsorted, uint32_t* cb,
+                                 const DevInstance* inst) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float3 c = f3(0.0f);
     bool ok = i < n;
@@ -71,7 +74,13 @@ __global__ void tri_boxes_kernel(const gbrt_vertex* V, const uint32_t* I, const 
         const float* a = V[pi.v_offset + I[io]].pos;
         const float* b = V[pi.v_offset + I[io + 1]].pos;
         const float* d = V[pi.v_offset + I[io + 2]].pos;
-        const float3 p0 = f3(a[0], a[1], a[2]), p1 = f3(b[0], b[1], b[2]), p2 = f3(d[0], d[1], d[2]);
+        float3 p0 = f3(a[0], a[1], a[2]), p1 = f3(b[0], b[1], b[2]), p2 = f3(d[0], d[1], d[2]);
+        if (inst && !inst[it.x].identity) {
+            const float* xf = inst[it.x].xf;
+            p0 = xform34_rn(xf, p0, 1.0f);
+            p1 = xform34_rn(xf, p1, 1.0f);
+            p2 = xform34_rn(xf, p2, 1.0f);
+        }
         const float3 l = fmin3(fmin3(p0, p1), p2), h = fmax3(fmax3(p0, p1), p2);
         lo[i] = f4(l, 0.0f);
         hi[i] = f4(h, 0.0f);
@@ -387,7 +396,7 @@ cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_ba
 
 cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
-                               uint32_t tri_base, BvhResult* res, cudaStream_t st) {
+                               uint32_t tri_base, BvhResult* res, cudaStream_t st, const DevInstance* inst) {
     if (n == 0) return cudaErrorInvalidValue;
     Scratch s;
     cudaError_t e = scratch_alloc(s, n, st);
@@ -396,7 +405,7 @@ cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indi
     if (e == cudaSuccess) {
         init_bounds_kernel<<<1, 32, 0, st>>>(s.cbounds);
         tri_boxes_kernel<<<blocks(n), 256, 0, st>>>(vertices, indices, prims, items, n, s.lo, s.hi, unsorted,
-                                                    s.cbounds);
+                                                    s.cbounds, inst);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
@@ -513,7 +522,7 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& bs, const gbrt_vertex
     if (s.cub_bytes > bs.sort_tmp_bytes) return cudaErrorInvalidValue;
     init_bounds_kernel<<<1, 32, 0, st>>>(s.cbounds);
     tri_boxes_kernel<<<blocks(n), 256, 0, st>>>(vertices, indices, prims, items, n, s.lo, s.hi, bs.unsorted,
-                                                s.cbounds);
+                                                s.cbounds, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
     if (e == cudaSuccess) {

@@ -37,9 +37,11 @@ double now_ms() {
     return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-// paths per batched wave: smaller than a single frame's waves so that a
-// wave, and the wait of a job that joins the batch, stays short
+// paths per batched wave: 2^22 while little work is queued, so that a wave,
+// and the wait of a job that joins the batch, stays short; growing to 2^24
+// (a quarter of the queued paths) when a deep queue makes throughput matter
 constexpr uint32_t kWaveCap = kMaxWavePaths < (1u << 22) ? kMaxWavePaths : (1u << 22);
+constexpr uint32_t kWaveCapDeep = kMaxWavePaths < (1u << 24) ? kMaxWavePaths : (1u << 24);
 constexpr uint32_t kChunkDiv = 8;             // pixel chunk = wave / 8 (finer packing)
 constexpr int kMaxInFlight = 2;
 
@@ -208,7 +210,10 @@ int JobQueue::pack_and_launch() {
     }
     w->njobs = w->nsegs = w->npaths = w->nfin = w->nb = 0;
     std::vector<Job*> finishing;
-    uint32_t room = std::min(kWaveCap, ctx->wf.cap);
+    uint64_t queued = 0;
+    for (const Job* j : order) queued += j->paths_left;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(queued / 4, kWaveCap), kWaveCapDeep);
+    uint32_t room = std::min(cap, ctx->wf.cap);
     for (Job* j : order) {
         if (w->njobs == (uint32_t)kMaxWaveJobs || w->nsegs == (uint32_t)kMaxWaveSegs || room == 0) break;
         const uint32_t slot = w->njobs, path0 = w->npaths;
@@ -457,7 +462,7 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
             const uint64_t gib = 1ull << 30;
             q->budget = c->jobs_budget ? c->jobs_budget : (fr > gib ? fr - gib : fr / 2);
             if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&q->dl, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = wavefront_reserve(c, kWaveCap, 0) == cudaSuccess ? cudaSuccess : cudaErrorMemoryAllocation;
+            if (e == cudaSuccess) e = wavefront_reserve(c, kWaveCapDeep, 0) == cudaSuccess ? cudaSuccess : cudaErrorMemoryAllocation;
             if (e != cudaSuccess) {
                 if (q->dl) cudaStreamDestroy(q->dl);
                 return cuda_fail(c, e, "job scheduler setup");

@@ -177,9 +177,12 @@ struct BvhResult {
 
 // Item descriptors for triangle BVHs: x = instance id (world BVH) or 0,
 // y = BLAS geometry id, z = primitive id, w = opaque flag.
+// inst (may be null): items whose instance is not an identity one are
+// transformed to world space (flattened instances).
 cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
-                               uint32_t tri_base, BvhResult* result_host, cudaStream_t st);
+                               uint32_t tri_base, BvhResult* result_host, cudaStream_t st,
+                               const DevInstance* inst = nullptr);
 
 // Scratch of one triangle-BVH build supplied by the caller instead of being
 // allocated (every pointer 256-byte aligned, sized for `capacity` items).
@@ -213,7 +216,8 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_v
 // the node count.
 cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  const uint4* items, uint32_t n, CwNode* nodes, TriRec* tris, uint32_t* nodes_used,
-                                 cudaStream_t st, std::vector<uint32_t>* level_starts = nullptr);
+                                 cudaStream_t st, std::vector<uint32_t>* level_starts = nullptr,
+                                 const DevInstance* inst = nullptr);
 // Refit of an 8-wide BVH built by build_triangle_cwbvh over the same
 // triangles: triangle records re-read from the vertices, then every node's
 // grid and child boxes recomputed level by level (level_starts: first node
@@ -221,7 +225,7 @@ cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* in
 // No host synchronisation.
 cudaError_t refit_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  CwNode* nodes, TriRec* tris, uint32_t ntris, const std::vector<uint32_t>& level_starts,
-                                 float4* boxes, cudaStream_t st);
+                                 float4* boxes, cudaStream_t st, const DevInstance* inst = nullptr);
 
 // TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
 // the instance ids.

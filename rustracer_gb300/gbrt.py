@@ -23,6 +23,7 @@ from . import types as T
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgbrt.so")
 
 OK, E_INVALID, E_CUDA, E_OOM, E_DEVICE_LIMIT, E_NOT_BUILT, E_NO_DEVICE, E_BUSY = 0, -1, -2, -3, -4, -5, -6, -7
+BUILD_NO_FLATTEN = 0x1
 MODE_AUTO, MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1, 2
 
 # name -> (restype, argtypes); every symbol include/gbrt.h declares
@@ -306,8 +307,9 @@ class Scene:
     textures), with create_as / create_top_as like
     crates/libs/asset_loader/src/acceleration_structures.rs."""
 
-    def __init__(self, ctx, sd, build=True):
+    def __init__(self, ctx, sd, build=True, build_flags=0):
         self.ctx, self.sd = ctx, sd
+        self.build_flags = build_flags
         L = ctx.L
         descs = (TexDesc * max(1, len(sd.textures)))()
         self._keep = []
@@ -329,7 +331,7 @@ class Scene:
     def create_as(self, ranges=None, instances=None):
         """BLAS per geometry, then the TLAS (create_as, acceleration_structures.rs:79-129)."""
         ranges = self.sd.geo_ranges if ranges is None else ranges
-        self.ctx.check(self.ctx.L.gbrt_blas_build(self.h, _p(ranges), len(ranges), 0))
+        self.ctx.check(self.ctx.L.gbrt_blas_build(self.h, _p(ranges), len(ranges), self.build_flags))
         self.create_top_as(instances)
 
     def create_top_as(self, instances=None):

@@ -120,13 +120,18 @@ def _instanced_scene(seed=31, ninst=40):
     return base
 
 
-def test_instanced_two_level(gpu_ctx):
+@pytest.mark.parametrize("flags", [0, 1], ids=["flattened", "tlas"])
+def test_instanced_two_level(gpu_ctx, flags):
+    """Transformed instances, flattened into the world BVH (default) or kept
+    in BLASes under a TLAS (GBRT_BUILD_NO_FLATTEN); the oracle follows the
+    same rule, so hits are bit-identical either way."""
+    import pyoracle as O
     from rustracer_gb300 import gbrt
     sd = _instanced_scene()
     rays = scenes.random_rays(30000, seed=32, origin_box=2.0)
-    ref, _ = oracle_scene(sd).trace(rays)
+    ref, _ = O.OracleScene(sd, build_flags=flags).trace(rays)
     assert len(np.unique(ref["instance_id"])) > 10
-    hits, _ = gbrt.Scene(gpu_ctx, sd).trace(rays)
+    hits, _ = gbrt.Scene(gpu_ctx, sd, build_flags=flags).trace(rays)
     assert_hits_equal(hits, ref)
 
 
