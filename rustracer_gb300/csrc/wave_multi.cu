@@ -58,14 +58,19 @@ __global__ void __launch_bounds__(128) wfm_camera(WfState st) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < c_wave.npaths; base += gridDim.x * blockDim.x)
         camera_body(MultiWave{}, st, base + threadIdx.x);
 }
+// A block starts on its own job's queue and then helps the other jobs'
+// queues (their fetch cursors are shared), so blocks of jobs that finish
+// early do not idle while a costlier job still has rays.
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_extend(WfState st, uint32_t b) {
-    extend_body<kMode>(MultiWave{}, st, b);
+    const uint32_t own = MultiWave{}.block_job(0), nj = c_wave.njobs;
+    for (uint32_t t = 0; t < nj; ++t) extend_body<kMode>(MultiWave{}, st, b, own + t < nj ? own + t : own + t - nj);
 }
 __global__ void __launch_bounds__(128) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_shadow(WfState st, uint32_t b) {
-    shadow_body<kMode>(MultiWave{}, st, b);
+    const uint32_t own = MultiWave{}.block_job(2), nj = c_wave.njobs;
+    for (uint32_t t = 0; t < nj; ++t) shadow_body<kMode>(MultiWave{}, st, b, own + t < nj ? own + t : own + t - nj);
 }
 __global__ void __launch_bounds__(128) wfm_finish(WfState st) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < c_wave.nfin; base += gridDim.x * blockDim.x)

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128) wf_camera(const __grid_constant__ SingleW
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode))
     wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
-    extend_body<kMode>(w, st, b);
+    extend_body<kMode>(w, st, b, 0u);
 }
 __global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     shade_body(w, st, b);
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ SingleWa
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode))
     wf_shadow(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
-    shadow_body<kMode>(w, st, b);
+    shadow_body<kMode>(w, st, b, 0u);
 }
 __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleWave w, WfState st) {
     finish_body(w, st, blockIdx.x * blockDim.x + threadIdx.x);

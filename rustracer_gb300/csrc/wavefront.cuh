@@ -120,8 +120,7 @@ GB_D void camera_body(const Wv& w, const WfState& st, uint32_t pid) {
 
 // traceRayEXT for the extension queue of bounce b (closest hit).
 template <int kMode, class Wv>
-GB_D void extend_body(const Wv& w, const WfState& st, uint32_t b) {
-    const uint32_t jb = w.block_job(0);
+GB_D void extend_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
     const WaveJob& J = w.job(jb);
     uint32_t* cnt = st.counts + jb * kWfCounters;
     const uint32_t n = cnt[kQueue + b], R = J.path0;
@@ -306,8 +305,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
 // Any-hit shadow rays of bounce b (castShadowRay, RayTracing.rchit:35-59),
 // then the deferred radiance update radiance += tp * (E [+ C if unoccluded]).
 template <int kMode, class Wv>
-GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b) {
-    const uint32_t jb = w.block_job(2);
+GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
     const WaveJob& J = w.job(jb);
     uint32_t* cnt = st.counts + jb * kWfCounters;
     const uint32_t n = cnt[kShadow + b], R = J.path0;
