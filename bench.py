@@ -468,7 +468,7 @@ def run_nrc(args):
     depth 12: device time until the running mean reaches relMSE <= 1e-2
     against a path-traced reference (--ref-spp samples), relMSE =
     mean((x - ref)^2 / (ref^2 + 1e-2)).  Plain path tracing adds 4 spp per
-    frame; the cache run adds 1 spp per frame and trains from scratch (its
+    frame; the cache run adds --nrc-spp per frame and trains from scratch (its
     training time is counted)."""
     from rustracer_gb300 import build, gbrt, workloads as WL
     build.build()
@@ -517,11 +517,12 @@ def run_nrc(args):
     losses = []
 
     def nrc_step(acc, spp):
-        r = cache.render(sc, sd.ubo(Wn, Hn, samples=1, total=spp + 1, bounces=depth, exposure=1.0, has_sky=True),
-                         acc, image=False, min_roughness=args.nrc_min_roughness, train_samples=1 << 16,
-                         train_steps=4)
+        k = args.nrc_spp
+        r = cache.render(sc, sd.ubo(Wn, Hn, samples=k, total=spp + k, bounces=depth, exposure=1.0, has_sky=True),
+                         acc, image=False, min_roughness=args.nrc_min_roughness, train_samples=args.nrc_samples,
+                         train_steps=args.nrc_steps)
         losses.append(r["loss"])
-        return float(r["stats"]["device_ms"]), int(r["stats"]["rays_total"]), 1
+        return float(r["stats"]["device_ms"]), int(r["stats"]["rays_total"]), k
 
     with ClockSampler(0) as clk:
         t_pt, pts_pt, rays_pt, tot_pt = curve(pt_step, args.max_frames)
@@ -536,7 +537,8 @@ def run_nrc(args):
                        "reference": f"{args.ref_spp} spp wavefront path tracing (FP32; an FP64 CPU reference at "
                                     f"this size does not fit the run)",
                        "cache": {"levels": 16, "table": 1 << 19, "features": 2, "mlp": "32-64x5-3 ReLU",
-                                 "train_samples_per_frame": 1 << 16, "adam_steps_per_frame": 4, "lr": 1e-3,
+                                 "spp_per_frame": args.nrc_spp, "train_samples_per_frame": args.nrc_samples,
+                                 "adam_steps_per_frame": args.nrc_steps, "lr": 1e-3,
                                  "min_roughness": args.nrc_min_roughness}},
             "plain_pt": {"time_s": None if t_pt is None else t_pt / 1e3, "curve": pts_pt[:: max(1, len(pts_pt) // 24)],
                          "mrays_per_s": rays_pt / tot_pt / 1e3},
@@ -595,6 +597,9 @@ def main():
     ap.add_argument("--ref-spp", type=int, default=1024, help="nrc: samples of the reference image")
     ap.add_argument("--max-frames", type=int, default=200, help="nrc: frame limit of the plain run (x4 for the cache)")
     ap.add_argument("--nrc-min-roughness", type=float, default=0.25, help="nrc: roughness a cache vertex needs")
+    ap.add_argument("--nrc-spp", type=int, default=4, help="nrc: samples per cache frame")
+    ap.add_argument("--nrc-samples", type=int, default=1 << 16, help="nrc: training samples per frame")
+    ap.add_argument("--nrc-steps", type=int, default=1, help="nrc: Adam steps per frame")
     args = ap.parse_args()
     global W, H, SPP, WORKLOAD
     if args.res:
