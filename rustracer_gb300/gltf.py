@@ -1,0 +1,353 @@
+"""glTF 2.0 -> the device-layout scene the C ABI takes (SceneData).
+
+Follows the reference's asset loader, step by step:
+* one geometry per triangle primitive with a POSITION attribute
+  (geometry.rs:100-267, is_primitive_supported :291-293), vertices laid out
+  like Vertex (pos.w = 0, uv0/uv1 default 0, colour default 1, tangent
+  default (1, 0, 0, 0), joints/weights default 0, skin_index -1), indices
+  generated when absent, normals generated per triangle when absent
+  (create_geo_normal, :270-289: the last triangle that touches a vertex
+  wins);
+* the geometry's material is the primitive's, material 0 when it has none
+  (DEFAULT_MATERIAL_INDEX);
+* materials packed like MaterialRaw::from (material.rs:130-381): texture
+  index + 1 (slot 0 is a 1x1 white texture), alpha cutoff 0.5 by default,
+  emissive (r, g, b, 0), ior 1.5 unless KHR_materials_ior, transmission /
+  volume / specular / specular-glossiness / unlit from their extensions;
+* textures: sRGB for colour textures, linear for normal, metallic-
+  roughness, transmission and specular textures (find_linear_textures,
+  material.rs:103-128), wrap modes from the sampler;
+* the default scene's node tree walked depth first from its root nodes
+  (scene_graph.rs:83-103); the whole scene scaled to 10 units along its
+  longest side and centred (load_scene, aabb.rs:65-69), node boxes
+  transformed by their min and max corners like Aabb * Mat4;
+* one instance per (node with a mesh, primitive) in that order, with the
+  node's world transform as a row-major 3x4, identity for skinned nodes,
+  custom index = geometry id, mask 0xFF, facing-cull disabled
+  (create_top_as, acceleration_structures.rs:136-172);
+* vertices of meshes used by skinned nodes get that skin's index
+  (duplicate_mesh_for_non_affine_transform, scene_graph.rs:191-235);
+* KHR_lights_punctual lights transformed by their node (light.rs:9-47,
+  spot lights as point lights); five zero-intensity point lights when the
+  scene has none and one zero-intensity directional light when it has none
+  (scene_graph.rs:55-81; the reference places the five at random, here
+  they are seeded).
+
+Not reproduced: mikktspace tangent generation for normal-mapped primitives
+without tangents (geometry.rs:197-212; tangents stay (1, 0, 0, 0)), JPEG
+textures (no decoder in this environment: such textures become the white
+slot), morph targets, cameras and animations.
+"""
+import base64
+import json
+import os
+import struct
+
+import numpy as np
+
+from . import types as T
+from .scenes import GeoBuilder, SceneData, identity_instances
+
+_COMP = {5120: np.int8, 5121: np.uint8, 5122: np.int16, 5123: np.uint16, 5125: np.uint32, 5126: np.float32}
+_NCOMP = {"SCALAR": 1, "VEC2": 2, "VEC3": 3, "VEC4": 4, "MAT2": 4, "MAT3": 9, "MAT4": 16}
+_WRAP = {33071: T.WRAP_CLAMP_TO_EDGE, 33648: T.WRAP_MIRRORED_REPEAT, 10497: T.WRAP_REPEAT}
+
+
+def _load(path):
+    """(json dict, list of buffer bytes) of a .gltf or .glb file."""
+    raw = open(path, "rb").read()
+    base = os.path.dirname(os.path.abspath(path))
+    glb_bin = None
+    if raw[:4] == b"glTF":
+        _, _, length = struct.unpack("<III", raw[:12])
+        pos, doc = 12, None
+        while pos < length:
+            n, kind = struct.unpack("<II", raw[pos:pos + 8])
+            body = raw[pos + 8:pos + 8 + n]
+            if kind == 0x4E4F534A:
+                doc = json.loads(body.decode("utf-8"))
+            elif kind == 0x004E4942:
+                glb_bin = body
+            pos += 8 + n
+    else:
+        doc = json.loads(raw.decode("utf-8"))
+    bufs = []
+    for b in doc.get("buffers", []):
+        uri = b.get("uri")
+        if uri is None:
+            bufs.append(glb_bin)
+        elif uri.startswith("data:"):
+            bufs.append(base64.b64decode(uri.split(",", 1)[1]))
+        else:
+            bufs.append(open(os.path.join(base, uri), "rb").read())
+    return doc, bufs, base
+
+
+def _accessor(doc, bufs, i):
+    a = doc["accessors"][i]
+    dt = np.dtype(_COMP[a["componentType"]])
+    nc = _NCOMP[a["type"]]
+    count = a["count"]
+    out = np.zeros((count, nc), dt)
+    if "bufferView" in a:
+        bv = doc["bufferViews"][a["bufferView"]]
+        data = bufs[bv["buffer"]]
+        off = bv.get("byteOffset", 0) + a.get("byteOffset", 0)
+        stride = bv.get("byteStride", 0) or dt.itemsize * nc
+        arr = np.ndarray((count, nc), dt, buffer=data, offset=off, strides=(stride, dt.itemsize))
+        out[:] = arr
+    if a.get("normalized") and dt != np.float32:
+        scale = float(np.iinfo(dt).max)
+        out = np.maximum(out.astype(np.float32) / scale, -1.0)
+    return out
+
+
+def _mat_of_node(node):
+    if "matrix" in node:
+        return np.array(node["matrix"], np.float64).reshape(4, 4).T  # column-major
+    t = np.array(node.get("translation", [0, 0, 0]), np.float64)
+    x, y, z, w = node.get("rotation", [0, 0, 0, 1])
+    s = np.array(node.get("scale", [1, 1, 1]), np.float64)
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    M = np.eye(4)
+    M[:3, :3] = R * s[None, :]
+    M[:3, 3] = t
+    return M
+
+
+def _texinfo(info):
+    if info is None:
+        return (-1, -1)
+    return (1 + int(info["index"]), int(info.get("texCoord", 0)))
+
+
+def _material(m):
+    raw = T.default_material()
+    pbr = m.get("pbrMetallicRoughness", {})
+    ext = m.get("extensions", {})
+    raw["alpha_mode"] = {"OPAQUE": T.ALPHA_OPAQUE, "MASK": T.ALPHA_MASK, "BLEND": T.ALPHA_BLEND}[m.get("alphaMode", "OPAQUE")]
+    raw["alpha_cutoff"] = m.get("alphaCutoff", 0.5)
+    raw["double_sided"] = int(bool(m.get("doubleSided", False)))
+    raw["base_color"] = pbr.get("baseColorFactor", [1, 1, 1, 1])
+    raw["base_color_texture"] = _texinfo(pbr.get("baseColorTexture"))
+    raw["metallic_factor"] = pbr.get("metallicFactor", 1.0)
+    raw["roughness_factor"] = pbr.get("roughnessFactor", 1.0)
+    raw["metallic_roughness_texture"] = _texinfo(pbr.get("metallicRoughnessTexture"))
+    raw["normal_texture"] = _texinfo(m.get("normalTexture"))
+    raw["emissive_texture"] = _texinfo(m.get("emissiveTexture"))
+    raw["emissive_factor"] = list(m.get("emissiveFactor", [0, 0, 0])) + [0.0]
+    raw["occlusion_texture"] = _texinfo(m.get("occlusionTexture"))
+    raw["ior"] = ext.get("KHR_materials_ior", {}).get("ior", 1.5)
+    raw["unlit"] = int("KHR_materials_unlit" in ext)
+    if "KHR_materials_transmission" in ext:
+        tr = ext["KHR_materials_transmission"]
+        raw["transmission_texture"] = _texinfo(tr.get("transmissionTexture"))
+        raw["transmission_factor"] = tr.get("transmissionFactor", 0.0)
+        raw["transmission_exist"] = 1
+    if "KHR_materials_volume" in ext:
+        vo = ext["KHR_materials_volume"]
+        raw["attenuation_color"] = vo.get("attenuationColor", [1, 1, 1])
+        raw["thickness_factor"] = vo.get("thicknessFactor", 0.0)
+        raw["thickness_texture"] = _texinfo(vo.get("thicknessTexture"))
+        raw["attenuation_distance"] = vo.get("attenuationDistance", np.finfo(np.float32).max)
+        raw["volume_exists"] = 1
+    if "KHR_materials_specular" in ext:
+        sp = ext["KHR_materials_specular"]
+        raw["specular_texture"] = _texinfo(sp.get("specularTexture"))
+        raw["specular_color_texture"] = _texinfo(sp.get("specularColorTexture"))
+        raw["specular_color_factor"] = list(sp.get("specularColorFactor", [1, 1, 1])) + [0.0]
+        raw["specular_factor"] = sp.get("specularFactor", 1.0)
+        raw["specular_exist"] = 1
+    if "KHR_materials_pbrSpecularGlossiness" in ext:
+        sg = ext["KHR_materials_pbrSpecularGlossiness"]
+        raw["workflow"] = 1
+        raw["sg_diffuse_factor"] = sg.get("diffuseFactor", [1, 1, 1, 1])
+        raw["sg_specular_glossiness_factor"] = list(sg.get("specularFactor", [1, 1, 1])) + [
+            sg.get("glossinessFactor", 1.0)]
+        raw["sg_diffuse_texture"] = _texinfo(sg.get("diffuseTexture"))
+        raw["sg_specular_glossiness_texture"] = _texinfo(sg.get("specularGlossinessTexture"))
+    return raw
+
+
+def _linear_images(doc):
+    lin = set()
+    tex = doc.get("textures", [])
+
+    def add(info):
+        if info is not None and "source" in tex[info["index"]]:
+            lin.add(tex[info["index"]]["source"])
+    for m in doc.get("materials", []):
+        add(m.get("normalTexture"))
+        add(m.get("pbrMetallicRoughness", {}).get("metallicRoughnessTexture"))
+        ext = m.get("extensions", {})
+        add(ext.get("KHR_materials_transmission", {}).get("transmissionTexture"))
+        add(ext.get("KHR_materials_specular", {}).get("specularTexture"))
+    return lin
+
+
+def _textures(doc, bufs, base):
+    from .png import read_png
+    white = (1, 1, T.TEX_RGBA8_SRGB, T.WRAP_REPEAT, T.WRAP_REPEAT, np.full((1, 1, 4), 255, np.uint8))
+    out = [white]
+    lin = _linear_images(doc)
+    images = doc.get("images", [])
+    samplers = doc.get("samplers", [])
+    for t in doc.get("textures", []):
+        smp = samplers[t["sampler"]] if "sampler" in t else {}
+        ws, wt = _WRAP[smp.get("wrapS", 10497)], _WRAP[smp.get("wrapT", 10497)]
+        src = t.get("source")
+        img = None
+        if src is not None:
+            im = images[src]
+            if "bufferView" in im:
+                bv = doc["bufferViews"][im["bufferView"]]
+                data = bufs[bv["buffer"]][bv.get("byteOffset", 0):bv.get("byteOffset", 0) + bv["byteLength"]]
+            elif im.get("uri", "").startswith("data:"):
+                data = base64.b64decode(im["uri"].split(",", 1)[1])
+            else:
+                data = open(os.path.join(base, im["uri"]), "rb").read()
+            if data[:8] == b"\x89PNG\r\n\x1a\n":
+                img = read_png(data)
+        if img is None:
+            out.append(white)
+            continue
+        fmt = T.TEX_RGBA8_UNORM if src in lin else T.TEX_RGBA8_SRGB
+        out.append((img.shape[1], img.shape[0], fmt, ws, wt, img))
+    return out
+
+
+def load(path, light_seed=0):
+    """Loads a .gltf / .glb file into SceneData (the arrays the C ABI takes)."""
+    doc, bufs, base = _load(path)
+    nodes = doc.get("nodes", [])
+    meshes = doc.get("meshes", [])
+    mats = doc.get("materials", [])
+    b = GeoBuilder()
+    for m in mats:
+        b.add_material(_material(m))
+    if not mats:
+        b.add_material(T.default_material())
+    # meshes -> geometries (one per supported primitive), object-space boxes
+    mesh_geos, mesh_box = [], []
+    for mesh in meshes:
+        geos, lo, hi = [], np.full(3, np.inf), np.full(3, -np.inf)
+        for p in mesh["primitives"]:
+            attrs = p["attributes"]
+            if "POSITION" not in attrs or p.get("mode", 4) != 4:
+                continue
+            pos = _accessor(doc, bufs, attrs["POSITION"]).astype(np.float32)
+            n = len(pos)
+            idx = (_accessor(doc, bufs, p["indices"]).reshape(-1).astype(np.uint32) if "indices" in p
+                   else np.arange(n, dtype=np.uint32))
+            if "NORMAL" in attrs:
+                nrm = _accessor(doc, bufs, attrs["NORMAL"]).astype(np.float32)
+            else:
+                nrm = np.zeros((n, 3), np.float32)
+                for t in idx.reshape(-1, 3):
+                    p0, p1, p2 = pos[t[0]], pos[t[1]], pos[t[2]]
+                    e0 = (p1 - p0) / np.linalg.norm(p1 - p0)
+                    e1 = (p2 - p0) / np.linalg.norm(p2 - p0)
+                    c = np.cross(e0, e1)
+                    nrm[t] = c / np.linalg.norm(c)
+            get = lambda k, dim: _accessor(doc, bufs, attrs[k]).astype(np.float32)[:, :dim] if k in attrs else None
+            color = None
+            if "COLOR_0" in attrs:
+                c = _accessor(doc, bufs, attrs["COLOR_0"]).astype(np.float32)
+                color = np.concatenate([c, np.ones((n, 1), np.float32)], 1) if c.shape[1] == 3 else c
+            base_v = b.add_vertices(pos, nrm, uv=get("TEXCOORD_0", 2), color=color, tangent=get("TANGENT", 4),
+                                    joints=_accessor(doc, bufs, attrs["JOINTS_0"]).astype(np.uint32)
+                                    if "JOINTS_0" in attrs else None,
+                                    weights=get("WEIGHTS_0", 4))
+            uv1 = get("TEXCOORD_1", 2)
+            if uv1 is not None:
+                b.vchunks[-1]["uv1"] = uv1
+            mat = p.get("material", 0)
+            geos.append(b.add_geometry(base_v, n, idx.reshape(-1, 3), mat))
+            lo, hi = np.minimum(lo, pos.min(0)), np.maximum(hi, pos.max(0))
+        mesh_geos.append(geos)
+        mesh_box.append((lo, hi) if geos else None)
+    # scene tree, normalisation
+    scene = doc.get("scenes", [{"nodes": list(range(len(nodes)))}])[doc.get("scene", 0)]
+    roots = scene.get("nodes", [])
+    local = [_mat_of_node(nd) for nd in nodes]
+
+    def node_box(i):
+        boxes = [node_box(c) for c in nodes[i].get("children", [])]
+        if "mesh" in nodes[i] and mesh_box[nodes[i]["mesh"]] is not None:
+            boxes.append(mesh_box[nodes[i]["mesh"]])
+        boxes = [bx for bx in boxes if bx is not None]
+        if not boxes:
+            return None
+        lo = np.min([bx[0] for bx in boxes], 0)
+        hi = np.max([bx[1] for bx in boxes], 0)
+        a = local[i] @ np.append(lo, 1.0)
+        c = local[i] @ np.append(hi, 1.0)
+        return np.minimum(a[:3], c[:3]), np.maximum(a[:3], c[:3])
+    boxes = [bx for bx in (node_box(r) for r in roots) if bx is not None]
+    norm = np.eye(4)
+    if boxes:
+        lo, hi = np.min([bx[0] for bx in boxes], 0), np.max([bx[1] for bx in boxes], 0)
+        size = hi - lo
+        side = size[0] if (size[0] > size[1] and size[0] > size[2]) else (size[1] if size[1] > size[2] else size[2])
+        scale = 10.0 / side if side > 0 else 1.0
+        norm = np.diag([scale, scale, scale, 1.0]) @ np.block([[np.eye(3), -(lo + size / 2)[:, None]],
+                                                               [np.zeros((1, 3)), np.ones((1, 1))]])
+    geos, xfs, dl, pl = [], [], [], []
+    lights = doc.get("extensions", {}).get("KHR_lights_punctual", {}).get("lights", [])
+    skinned_meshes = {}
+
+    def walk(i, parent):
+        world = parent @ local[i]
+        nd = nodes[i]
+        if "mesh" in nd:
+            m = nd["mesh"]
+            if "skin" in nd:
+                skinned_meshes.setdefault(m, nd["skin"])
+            xf = np.eye(4) if "skin" in nd else world
+            for g in mesh_geos[m]:
+                geos.append(g)
+                xfs.append(xf[:3, :4].astype(np.float32).reshape(12))
+        li = nd.get("extensions", {}).get("KHR_lights_punctual", {}).get("light")
+        if li is not None:
+            L = lights[li]
+            raw = np.zeros((), T.LIGHT)
+            raw["color"] = list(L.get("color", [1, 1, 1])) + [0.0]
+            kind = L.get("type", "point")
+            v = world @ (np.array([0, 0, -1.0, 0]) if kind == "directional" else np.array([0, 0, 0, 1.0]))
+            raw["transform"] = v.astype(np.float32)
+            raw["kind"] = 0 if kind == "directional" else 1
+            raw["range"] = L.get("range", np.finfo(np.float32).max)
+            raw["intensity"] = L.get("intensity", 1.0)
+            (dl if kind == "directional" else pl).append(raw)
+        for c in nd.get("children", []):
+            walk(c, world)
+    for r in roots:
+        walk(r, norm)
+    # skin indices of meshes used by skinned nodes
+    for m, skin in skinned_meshes.items():
+        for g in mesh_geos[m]:
+            p = b.prims[g]
+            off, n = int(p["v_offset"]), int(b.ranges[g]["v_len"])
+            verts = np.concatenate(b.vchunks)
+            verts["skin_index"][off:off + n] = skin
+            b.vchunks = [verts]
+    if not pl:
+        rng = np.random.default_rng(light_seed)
+        for _ in range(5):
+            raw = np.zeros((), T.LIGHT)
+            raw["color"] = (1, 1, 1, 1)
+            raw["transform"] = ((rng.random(4) - 0.5) * 2.0 * 10.0).astype(np.float32)
+            raw["kind"] = 1
+            raw["range"] = np.inf
+            raw["intensity"] = 0.0
+            pl.append(raw)
+    if not dl:
+        dl.append(T.default_dir_light())
+    inst = identity_instances(geos, transforms=xfs)
+    sd = b.finish(instances=inst, dlights=np.array(dl, T.LIGHT), plights=np.array(pl, T.LIGHT),
+                  textures=_textures(doc, bufs, base),
+                  camera=dict(eye=(0.0, 0.0, 12.0), direction=(0.0, 0.0, -1.0), fov_deg=60.0),
+                  name=os.path.basename(path))
+    return sd
