@@ -33,10 +33,19 @@ Follows the reference's asset loader, step by step:
   (scene_graph.rs:55-81; the reference places the five at random, here
   they are seeded).
 
+Animation (GltfScene.animate / instances / skins) follows animation.rs and
+skinning.rs: every channel's time wraps into [first key, last key), the key
+segment is found by a linear scan, translation and scale interpolate
+linearly, by step or by cubic Hermite spline (glTF in / value / out
+tangents), rotations by slerp (also for cubic splines) or step; the node's
+TRS takes the channel's output and the world transforms are recomputed; a
+skin's joint matrices are world(joint) x inverse bind matrix, column-major,
+256 slots with zero matrices past the last joint.
+
 Not reproduced: mikktspace tangent generation for normal-mapped primitives
 without tangents (geometry.rs:197-212; tangents stay (1, 0, 0, 0)), JPEG
 textures (no decoder in this environment: such textures become the white
-slot), morph targets, cameras and animations.
+slot), morph targets and cameras.
 """
 import base64
 import json
@@ -102,19 +111,83 @@ def _accessor(doc, bufs, i):
     return out
 
 
-def _mat_of_node(node):
-    if "matrix" in node:
-        return np.array(node["matrix"], np.float64).reshape(4, 4).T  # column-major
-    t = np.array(node.get("translation", [0, 0, 0]), np.float64)
-    x, y, z, w = node.get("rotation", [0, 0, 0, 1])
-    s = np.array(node.get("scale", [1, 1, 1]), np.float64)
+def _trs_matrix(t, q, s):
+    x, y, z, w = q
     R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
                   [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
                   [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
     M = np.eye(4)
-    M[:3, :3] = R * s[None, :]
+    M[:3, :3] = R * np.asarray(s, np.float64)[None, :]
     M[:3, 3] = t
     return M
+
+
+def _mat_of_node(node):
+    if "matrix" in node:
+        return np.array(node["matrix"], np.float64).reshape(4, 4).T  # column-major
+    return _trs_matrix(np.array(node.get("translation", [0, 0, 0]), np.float64), node.get("rotation", [0, 0, 0, 1]),
+                       node.get("scale", [1, 1, 1]))
+
+
+def _decompose(M):
+    """TRS of an affine matrix (for matrix nodes that get animated)."""
+    t = M[:3, 3].copy()
+    s = np.linalg.norm(M[:3, :3], axis=0)
+    R = M[:3, :3] / np.where(s == 0, 1, s)[None, :]
+    w = np.sqrt(max(0.0, 1 + R[0, 0] + R[1, 1] + R[2, 2])) / 2
+    x = np.sqrt(max(0.0, 1 + R[0, 0] - R[1, 1] - R[2, 2])) / 2
+    y = np.sqrt(max(0.0, 1 - R[0, 0] + R[1, 1] - R[2, 2])) / 2
+    z = np.sqrt(max(0.0, 1 - R[0, 0] - R[1, 1] + R[2, 2])) / 2
+    x = np.copysign(x, R[2, 1] - R[1, 2])
+    y = np.copysign(y, R[0, 2] - R[2, 0])
+    z = np.copysign(z, R[1, 0] - R[0, 1])
+    return t, np.array([x, y, z, w]), s
+
+
+def _slerp(a, b, f):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    d = float(np.dot(a, b))
+    if d < 0:
+        b, d = -b, -d
+    if d > 0.9995:
+        q = a + (b - a) * f
+        return q / np.linalg.norm(q)
+    th = np.arccos(d)
+    return (np.sin((1 - f) * th) * a + np.sin(f * th) * b) / np.sin(th)
+
+
+def _hermite(p0, m0, p1, m1, t):
+    t2, t3 = t * t, t * t * t
+    return (2 * t3 - 3 * t2 + 1) * p0 + (t3 - 2 * t2 + t) * m0 + (-2 * t3 + 3 * t2) * p1 + (t3 - t2) * m1
+
+
+class _Channel:
+    def __init__(self, node, path, times, values, interp):
+        self.node, self.path, self.times, self.values, self.interp = node, path, times, values, interp
+
+    def sample(self, t):
+        inp = self.times
+        lo, hi = inp[0], inp[-1]
+        if t > lo and hi > lo:
+            t = (t - lo) % (hi - lo) + lo
+        s = e = 0
+        for i in range(len(inp) - 1):
+            if inp[i] <= t <= inp[i + 1]:
+                s, e = i, i + 1
+        pt, nt = inp[s], inp[e]
+        f = (t - pt) / (nt - pt) if nt > pt else 0.0
+        v = self.values
+        if self.interp == "CUBICSPLINE":
+            key = lambda k: v[3 * k:3 * k + 3]  # in tangent, value, out tangent
+            if self.path == "rotation":
+                return _slerp(key(s)[1], key(e)[1], f)
+            dt = nt - pt
+            return _hermite(key(s)[1], dt * key(s)[2], key(e)[1], dt * key(e)[0], f)
+        if self.interp == "STEP":
+            return v[s]
+        if self.path == "rotation":
+            return _slerp(v[s], v[e], f)
+        return v[s] + (v[e] - v[s]) * f
 
 
 def _texinfo(info):
@@ -294,37 +367,27 @@ def load(path, light_seed=0):
         scale = 10.0 / side if side > 0 else 1.0
         norm = np.diag([scale, scale, scale, 1.0]) @ np.block([[np.eye(3), -(lo + size / 2)[:, None]],
                                                                [np.zeros((1, 3)), np.ones((1, 1))]])
-    geos, xfs, dl, pl = [], [], [], []
     lights = doc.get("extensions", {}).get("KHR_lights_punctual", {}).get("lights", [])
+    state = GltfScene(doc, bufs, local, roots, norm, mesh_geos)
+    world = state.world()
+    dl, pl = [], []
     skinned_meshes = {}
-
-    def walk(i, parent):
-        world = parent @ local[i]
+    for i in state.order:
         nd = nodes[i]
-        if "mesh" in nd:
-            m = nd["mesh"]
-            if "skin" in nd:
-                skinned_meshes.setdefault(m, nd["skin"])
-            xf = np.eye(4) if "skin" in nd else world
-            for g in mesh_geos[m]:
-                geos.append(g)
-                xfs.append(xf[:3, :4].astype(np.float32).reshape(12))
+        if "mesh" in nd and "skin" in nd:
+            skinned_meshes.setdefault(nd["mesh"], nd["skin"])
         li = nd.get("extensions", {}).get("KHR_lights_punctual", {}).get("light")
         if li is not None:
             L = lights[li]
             raw = np.zeros((), T.LIGHT)
             raw["color"] = list(L.get("color", [1, 1, 1])) + [0.0]
             kind = L.get("type", "point")
-            v = world @ (np.array([0, 0, -1.0, 0]) if kind == "directional" else np.array([0, 0, 0, 1.0]))
+            v = world[i] @ (np.array([0, 0, -1.0, 0]) if kind == "directional" else np.array([0, 0, 0, 1.0]))
             raw["transform"] = v.astype(np.float32)
             raw["kind"] = 0 if kind == "directional" else 1
             raw["range"] = L.get("range", np.finfo(np.float32).max)
             raw["intensity"] = L.get("intensity", 1.0)
             (dl if kind == "directional" else pl).append(raw)
-        for c in nd.get("children", []):
-            walk(c, world)
-    for r in roots:
-        walk(r, norm)
     # skin indices of meshes used by skinned nodes
     for m, skin in skinned_meshes.items():
         for g in mesh_geos[m]:
@@ -345,9 +408,112 @@ def load(path, light_seed=0):
             pl.append(raw)
     if not dl:
         dl.append(T.default_dir_light())
-    inst = identity_instances(geos, transforms=xfs)
+    inst = state.instances()
     sd = b.finish(instances=inst, dlights=np.array(dl, T.LIGHT), plights=np.array(pl, T.LIGHT),
                   textures=_textures(doc, bufs, base),
                   camera=dict(eye=(0.0, 0.0, 12.0), direction=(0.0, 0.0, -1.0), fov_deg=60.0),
                   name=os.path.basename(path))
+    sd.gltf = state  # animation state: sd.gltf.animate(t), .instances(), .skins()
     return sd
+
+
+class GltfScene:
+    """Node tree, animations and skins of a loaded glTF (scene_graph.rs,
+    animation.rs, skinning.rs): animate(t) moves the animated nodes,
+    instances() gives the TLAS instances for gbrt_tlas_update and skins() the
+    joint matrices for gbrt_skin_and_refit."""
+
+    def __init__(self, doc, bufs, local, roots, norm, mesh_geos):
+        self.nodes = doc.get("nodes", [])
+        self.local = [m.copy() for m in local]
+        self.roots, self.norm, self.mesh_geos = roots, norm, mesh_geos
+        self.order = []  # depth-first pre-order from the roots
+        stack = list(reversed(roots))
+        while stack:
+            i = stack.pop()
+            self.order.append(i)
+            stack.extend(reversed(self.nodes[i].get("children", [])))
+        self.trs = {}
+        self.channels = []
+        for an in doc.get("animations", []):
+            for ch in an.get("channels", []):
+                tgt = ch.get("target", {})
+                path = tgt.get("path")
+                if "node" not in tgt or path not in ("translation", "rotation", "scale"):
+                    continue  # morph weights are ignored, as in the reference
+                smp = an["samplers"][ch["sampler"]]
+                times = _accessor(doc, bufs, smp["input"]).reshape(-1).astype(np.float64)
+                vals = _accessor(doc, bufs, smp["output"]).astype(np.float64)
+                self.channels.append(_Channel(tgt["node"], path, times, vals, smp.get("interpolation", "LINEAR")))
+        self.skin_joints = []
+        for sk in doc.get("skins", []):
+            joints = sk["joints"]
+            ibm = (_accessor(doc, bufs, sk["inverseBindMatrices"]).reshape(-1, 4, 4).transpose(0, 2, 1)
+                   if "inverseBindMatrices" in sk else np.tile(np.eye(4), (len(joints), 1, 1)))
+            self.skin_joints.append((joints, ibm.astype(np.float64)))
+
+    def world(self):
+        w = {}
+
+        def rec(i, parent):
+            w[i] = parent @ self.local[i]
+            for c in self.nodes[i].get("children", []):
+                rec(c, w[i])
+        for r in self.roots:
+            rec(r, self.norm)
+        return w
+
+    def animate(self, t):
+        """Applies every channel at time t (seconds)."""
+        for ch in self.channels:
+            i = ch.node
+            if i not in self.trs:
+                self.trs[i] = list(_decompose(self.local[i]))
+            k = {"translation": 0, "rotation": 1, "scale": 2}[ch.path]
+            self.trs[i][k] = np.asarray(ch.sample(t), np.float64)
+        for i, (tt, q, sc) in self.trs.items():
+            self.local[i] = _trs_matrix(tt, q, sc)
+
+    def instances(self):
+        w = self.world()
+        geos, xfs = [], []
+        for i in self.order:
+            nd = self.nodes[i]
+            if "mesh" not in nd:
+                continue
+            xf = np.eye(4) if "skin" in nd else w[i]
+            for g in self.mesh_geos[nd["mesh"]]:
+                geos.append(g)
+                xfs.append(xf[:3, :4].astype(np.float32).reshape(12))
+        return identity_instances(geos, transforms=xfs)
+
+    def skins(self):
+        w = self.world()
+        out = np.zeros(max(1, len(self.skin_joints)), T.SKIN)
+        for k, (joints, ibm) in enumerate(self.skin_joints):
+            for j, node in enumerate(joints[:256]):
+                out[k]["joints"][j] = (w[node] @ ibm[j]).T.reshape(16).astype(np.float32)
+        return out
+
+
+_FACE_ALIASES = {"posx": 0, "negx": 1, "posy": 2, "negy": 3, "posz": 4, "negz": 5,
+                 "right": 0, "left": 1, "top": 2, "bottom": 3, "front": 4, "back": 5}
+
+
+def load_cubemap(directory):
+    """Six square PNG faces named like the reference's skybox directories
+    (posx/negx/... or right/left/top/bottom/front/back, cubumap.rs Face) ->
+    (face size, RGBA8 bytes in +X, -X, +Y, -Y, +Z, -Z order) for
+    gbrt_skybox_set."""
+    from .png import read_png
+    faces = [None] * 6
+    for name in os.listdir(directory):
+        stem, ext = os.path.splitext(name)
+        if ext.lower() == ".png" and stem in _FACE_ALIASES:
+            faces[_FACE_ALIASES[stem]] = read_png(open(os.path.join(directory, name), "rb").read())
+    if any(f is None for f in faces):
+        raise ValueError("a cubemap needs six PNG faces")
+    size = faces[0].shape[0]
+    if any(f.shape[:2] != (size, size) for f in faces):
+        raise ValueError("cubemap faces must be square and of one size")
+    return size, np.concatenate([f.reshape(-1) for f in faces])

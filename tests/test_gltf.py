@@ -38,8 +38,12 @@ def _write_gltf(path, tex_png):
     tri = np.array([[0, 0, 0], [2, 0, 0], [0, 0, 2]], np.float32)
     joints = np.array([[1, 2, 0, 0]] * 3, np.uint16)
     weights = np.array([[0.5, 0.5, 0, 0]] * 3, np.float32)
+    times = np.array([0, 1, 2], np.float32)
+    trans = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0]], np.float32)
+    rots = np.array([[0, 0, 0, 1], [0, 0, 0.7071067811865476, 0.7071067811865476], [0, 0, 1, 0]], np.float32)
+    ibm = np.stack([np.eye(4), np.diag([2.0, 2.0, 2.0, 1.0])]).astype(np.float32)  # column-major = row-major here
     blobs = [quad.tobytes(), quv.tobytes(), qidx.tobytes() + b"\0\0", tri.tobytes(), joints.tobytes(),
-             weights.tobytes(), tex_png]
+             weights.tobytes(), times.tobytes(), trans.tobytes(), rots.tobytes(), ibm.tobytes(), tex_png]
     views, off = [], 0
     for bl in blobs:
         views.append({"buffer": 0, "byteOffset": off, "byteLength": len(bl)})
@@ -52,13 +56,17 @@ def _write_gltf(path, tex_png):
         {"bufferView": 3, "componentType": 5126, "count": 3, "type": "VEC3", "min": [0, 0, 0], "max": [2, 0, 2]},
         {"bufferView": 4, "componentType": 5123, "count": 3, "type": "VEC4"},
         {"bufferView": 5, "componentType": 5126, "count": 3, "type": "VEC4"},
+        {"bufferView": 6, "componentType": 5126, "count": 3, "type": "SCALAR"},
+        {"bufferView": 7, "componentType": 5126, "count": 3, "type": "VEC3"},
+        {"bufferView": 8, "componentType": 5126, "count": 3, "type": "VEC4"},
+        {"bufferView": 9, "componentType": 5126, "count": 2, "type": "MAT4"},
     ]
     doc = {
         "asset": {"version": "2.0"},
         "buffers": [{"byteLength": len(buf), "uri": "data:application/octet-stream;base64," +
                      base64.b64encode(buf).decode()}],
         "bufferViews": views, "accessors": acc,
-        "images": [{"bufferView": 6, "mimeType": "image/png"}],
+        "images": [{"bufferView": 10, "mimeType": "image/png"}],
         "samplers": [{"wrapS": 33071, "wrapT": 33648}],
         "textures": [{"source": 0, "sampler": 0}],
         "materials": [
@@ -83,6 +91,11 @@ def _write_gltf(path, tex_png):
         ],
         "extensions": {"KHR_lights_punctual": {"lights": [{"type": "point", "color": [1, 0.5, 0.5], "intensity": 7}]}},
         "scenes": [{"nodes": [0, 3, 4]}], "scene": 0,
+        "skins": [{"joints": [1, 2], "inverseBindMatrices": 9}],
+        "animations": [{"samplers": [{"input": 6, "output": 7, "interpolation": "LINEAR"},
+                                     {"input": 6, "output": 8, "interpolation": "STEP"}],
+                        "channels": [{"sampler": 0, "target": {"node": 1, "path": "translation"}},
+                                     {"sampler": 1, "target": {"node": 2, "path": "rotation"}}]}],
     }
     with open(path, "w") as f:
         json.dump(doc, f)
@@ -156,3 +169,42 @@ def test_reference_cornell_asset():
     size = world.max(0) - world.min(0)
     assert abs(size.max() - 10.0) < 0.2  # scene scaled to 10 units along its longest side
     assert len(sd.plights) == 5 and np.all(sd.plights["intensity"] == 0)  # no lights in the file
+
+
+def test_gltf_animation_and_skins(tmp_path):
+    tex = np.full((1, 1, 4), 255, np.uint8)
+    png.write_png(str(tmp_path / "t.png"), tex)
+    _write_gltf(str(tmp_path / "s.gltf"), (tmp_path / "t.png").read_bytes())
+    sd = gltf.load(str(tmp_path / "s.gltf"))
+    g = sd.gltf
+    norm = g.norm
+    # node 1 (the quad) is translated by the channel: (0.5, 0, 0) at t = 0.5,
+    # (1, 0.5, 0) at t = 1.5, and t = 2.5 wraps to 0.5
+    for t, tr in ((0.5, [0.5, 0, 0]), (1.5, [1, 0.5, 0]), (2.5, [0.5, 0, 0])):
+        g.animate(t)
+        xf = g.instances()["transform"].reshape(-1, 3, 4)[0]
+        expect = norm @ np.array([[1, 0, 0, 1], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1.0]]) @ \
+            np.block([[np.eye(3) * 2, np.array(tr, float)[:, None]], [np.zeros((1, 3)), np.ones((1, 1))]])
+        assert np.allclose(xf, expect[:3], atol=1e-5), t
+    # node 2 rotation by STEP: key 1 (90 degrees about z) holds on [1, 2)
+    g.animate(1.5)
+    w = g.world()
+    R = w[2][:3, :3] / norm[0, 0]
+    assert np.allclose(R, [[0, -1, 0], [1, 0, 0], [0, 0, 1]], atol=1e-6)
+    # joint matrices: world(joint) x inverse bind matrix, column-major; unused slots zero
+    sk = g.skins()
+    assert sk.shape == (1,)
+    m0 = sk[0]["joints"][0].reshape(4, 4).T
+    m1 = sk[0]["joints"][1].reshape(4, 4).T
+    assert np.allclose(m0, w[1], atol=1e-5)
+    assert np.allclose(m1, w[2] @ np.diag([2.0, 2.0, 2.0, 1.0]), atol=1e-5)
+    assert np.all(sk[0]["joints"][2:] == 0)
+
+
+def test_cubemap_faces(tmp_path):
+    names = ["right", "left", "top", "bottom", "front", "back"]
+    for k, n in enumerate(names):
+        png.write_png(str(tmp_path / f"{n}.png"), np.full((4, 4, 4), 10 * k, np.uint8))
+    size, data = gltf.load_cubemap(str(tmp_path))
+    assert size == 4 and data.size == 6 * 4 * 4 * 4
+    assert [int(data[k * 64]) for k in range(6)] == [0, 10, 20, 30, 40, 50]
