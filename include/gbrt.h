@@ -511,7 +511,8 @@ int gbrt_jobs_configure(gbrt_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t polic
  * multiresolution hash-grid encoding (16 levels x 2^log2_table entries x 2
  * features) and an MLP 32 -> 5 x 64 (ReLU) -> 3, trained online on path
  * suffixes.  Queries run the MLP on tensor cores in BF16 with FP32
- * accumulation; training runs in FP32 with Adam (b1 0.9, b2 0.99, eps 1e-15)
+ * accumulation: tcgen05.mma with the accumulator in tensor memory by
+ * default, mma.sync with GBRT_NRC_QUERY_MMA_SYNC; training runs in FP32 with Adam (b1 0.9, b2 0.99, eps 1e-15)
  * on the loss mean((y - t)^2 / (y^2 + 0.01)) (y not differentiated in the
  * denominator).  Positions are normalised to [box_lo, box_hi]. */
 typedef struct gbrt_nrc gbrt_nrc;
@@ -523,7 +524,10 @@ typedef struct gbrt_nrc_config {
     float learning_rate;       /* Adam step size (1e-2) */
     float box_lo[3], box_hi[3];
     uint64_t seed;             /* parameter initialisation */
+    uint32_t flags;            /* 0: queries on tcgen05; GBRT_NRC_QUERY_MMA_SYNC: on mma.sync */
+    uint32_t _pad;
 } gbrt_nrc_config;
+#define GBRT_NRC_QUERY_MMA_SYNC 0x1u
 
 int gbrt_nrc_create(gbrt_ctx* ctx, const gbrt_nrc_config* cfg, gbrt_nrc** out);
 int gbrt_nrc_destroy(gbrt_nrc* nrc);

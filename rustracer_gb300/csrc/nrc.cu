@@ -184,6 +184,203 @@ __global__ void __launch_bounds__(128) nrc_infer_kernel(NrcView v, const float4*
     }
 }
 
+// ---------------------------------------------------------------------------
+// Queries on the 5th-generation tensor cores (tcgen05).  A CTA of 128 threads
+// takes 128 queries per step: thread i encodes query i into row i of the A
+// tile (shared memory, BF16, K-major canonical layout without swizzle: 8x8
+// core matrices of 128 B, K-adjacent ones 128 B apart, 8-row groups K*16 B
+// apart); one elected thread issues the layer's tcgen05.mma (M = 128, N = 64
+// or 16, K = 16 per instruction) with the FP32 accumulator in tensor memory
+// (64 columns), commits to an mbarrier, and every warp reads its 32 rows back
+// with tcgen05.ld, applies ReLU, and writes them as the next layer's A tile.
+// Weights stay in shared memory in the same layout for the whole kernel.
+// Every wait is bounded: on a timeout the kernel records kTcTimeout in
+// *status and stops issuing work.
+
+constexpr uint32_t kTcTimeout = 1u;
+constexpr int kTcRows = 128;
+// BF16 weights in core-matrix layout: layer l occupies out_l x in_l (W5 padded to 16 rows)
+__host__ __device__ constexpr int tc_w_off(int l) {  // in elements
+    return l == 0 ? 0 : kNrcHidden * kNrcIn + (l - 1) * kNrcHidden * kNrcHidden;
+}
+constexpr int kTcWElems = tc_w_off(5) + 16 * kNrcHidden;                    // 19,456
+constexpr size_t kTcSmem = (size_t)kTcWElems * 2 + (size_t)kTcRows * kNrcHidden * 2 + 64;
+
+// byte offset of element (row, k) in a K-major no-swizzle tile with K columns
+GB_D uint32_t tc_core_off(uint32_t row, uint32_t k, uint32_t K) {
+    return ((row >> 3) * (K >> 3) + (k >> 3)) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Shared-memory matrix descriptor: start >> 4 (bits 0-13), leading (K)
+// byte offset >> 4 (16-29), stride (8-row group) byte offset >> 4 (32-45),
+// version 1 (46-47), no swizzle (61-63 = 0).
+GB_D uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
+// A and B (7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t M, uint32_t N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+GB_D void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+GB_D bool tc_wait(uint32_t mbar, uint32_t phase) {
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+#define TC_LD16(base, v)                                                                                        \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, " \
+                 "[%16];\n"                                                                                     \
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),          \
+                   "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),      \
+                   "=r"(v[14]), "=r"(v[15])                                                                     \
+                 : "r"(base))
+
+__global__ void __launch_bounds__(128, 1) nrc_infer_tc_kernel(NrcView v, const float4* __restrict__ q, uint32_t n,
+                                                              float4* __restrict__ out, const uint32_t* n_dev,
+                                                              const __nv_bfloat16* __restrict__ wtc,
+                                                              uint32_t* status) {
+    extern __shared__ __align__(16) unsigned char smem_tc[];
+    unsigned char* sw = smem_tc;                             // weights
+    unsigned char* sa = smem_tc + (size_t)kTcWElems * 2;     // A tile, 128 x 64 BF16
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sa + kTcRows * kNrcHidden * 2);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    if (n_dev) n = min(n, *n_dev);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    {  // weights are pre-arranged in core-matrix order by the host
+        const uint4* src = reinterpret_cast<const uint4*>(wtc);
+        uint4* dst = reinterpret_cast<uint4*>(sw);
+        for (int i = tid; i < kTcWElems / 8; i += blockDim.x) dst[i] = src[i];
+    }
+    const uint32_t sw_s = (uint32_t)__cvta_generic_to_shared(sw), sa_s = (uint32_t)__cvta_generic_to_shared(sa);
+    const uint32_t mbar_s = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_s));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(tslot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(dst));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t tlane = tmem + ((warp * 32u) << 16);  // this warp's 32 lanes
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+        const uint32_t i = base + tid;
+        {
+            float x[kNrcIn];
+            const float4 qi = i < n ? q[i] : f4(0.0f, 0.0f, 0.0f, 0.0f);
+            nrc_encode_h(v, nrc_normalise(v, f3(qi)), x);
+#pragma unroll
+            for (int k = 0; k < kNrcIn; k += 8) {
+                uint4 pk;
+                pk.x = pack_bf16(x[k], x[k + 1]);
+                pk.y = pack_bf16(x[k + 2], x[k + 3]);
+                pk.z = pack_bf16(x[k + 4], x[k + 5]);
+                pk.w = pack_bf16(x[k + 6], x[k + 7]);
+                *reinterpret_cast<uint4*>(sa + tc_core_off(tid, k, kNrcIn)) = pk;
+            }
+        }
+        float y[3] = {0.0f, 0.0f, 0.0f};
+        for (int l = 0; l < 6 && ok; ++l) {
+            const uint32_t K = l == 0 ? kNrcIn : kNrcHidden, N = l == 5 ? 16 : kNrcHidden;
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (tid == 0) {
+                const uint32_t wbase = sw_s + (uint32_t)tc_w_off(l) * 2u;
+                for (uint32_t ks = 0; ks < K / 16; ++ks) {
+                    const uint64_t ad = tc_smem_desc(sa_s + ks * 256u, 128u, K * 16u);
+                    const uint64_t bd = tc_smem_desc(wbase + ks * 256u, 128u, K * 16u);
+                    tc_mma(tmem, ad, bd, tc_idesc(kTcRows, N), ks);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    mbar_s)
+                             : "memory");
+            }
+            ok = __syncthreads_and(tc_wait(mbar_s, phase) ? 1 : 0) != 0;  // uniform across the CTA
+            phase ^= 1u;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (l < 5) {
+#pragma unroll
+                for (int c = 0; c < kNrcHidden; c += 16) {
+                    uint32_t r[16];
+                    TC_LD16(tlane + (uint32_t)c, r);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int k = 0; k < 16; k += 8) {
+                        uint4 pk;
+                        pk.x = pack_bf16(fmaxf(__uint_as_float(r[k]), 0.0f), fmaxf(__uint_as_float(r[k + 1]), 0.0f));
+                        pk.y = pack_bf16(fmaxf(__uint_as_float(r[k + 2]), 0.0f), fmaxf(__uint_as_float(r[k + 3]), 0.0f));
+                        pk.z = pack_bf16(fmaxf(__uint_as_float(r[k + 4]), 0.0f), fmaxf(__uint_as_float(r[k + 5]), 0.0f));
+                        pk.w = pack_bf16(fmaxf(__uint_as_float(r[k + 6]), 0.0f), fmaxf(__uint_as_float(r[k + 7]), 0.0f));
+                        *reinterpret_cast<uint4*>(sa + tc_core_off(tid, c + k, kNrcHidden)) = pk;
+                    }
+                }
+            } else {
+                uint32_t r[16];
+                TC_LD16(tlane, r);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                y[0] = __uint_as_float(r[0]);
+                y[1] = __uint_as_float(r[1]);
+                y[2] = __uint_as_float(r[2]);
+            }
+        }
+        if (ok && i < n) out[i] = f4(y[0], y[1], y[2], q[i].w);
+    }
+    if (!ok) {
+        if (status && tid == 0) atomicOr(status, kTcTimeout);
+        tc_wait(mbar_s, phase ^ 1u);  // give the MMAs still in flight (bounded) time before the columns are freed
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
+}
+
+// FP32 masters -> BF16 weights in the core-matrix order of the tcgen05
+// kernel (W5 padded to 16 rows with zeros).
+__global__ void nrc_tc_weights_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ wtc) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kTcWElems) return;
+    int l = 0;
+    while (l < 5 && e >= tc_w_off(l + 1)) ++l;
+    const int K = l == 0 ? kNrcIn : kNrcHidden;
+    const int local = e - tc_w_off(l);
+    // invert tc_core_off: 128-B core matrices of 8 rows x 8 elements
+    const int cm = local / 64, within = local % 64;
+    const int kc = cm % (K / 8), rg = cm / (K / 8);
+    const int row = rg * 8 + within / 8, k = kc * 8 + within % 8;
+    const int O = l == 5 ? kNrcOut : kNrcHidden;
+    const float x = row < O ? w[f32_off(l) + row * K + k] : 0.0f;
+    wtc[e] = __float2bfloat16_rn(x);
+}
+
 struct NrcGrad {
     float* grid;  // [levels * table * 2]
     float* mlp;   // [kNrcMlpParams]
@@ -409,8 +606,9 @@ struct gbrt_nrc {
     DevBuf grid_w, grid_h, grid_g, grid_m, grid_v;
     DevBuf mlp_w, mlp_h, mlp_g, mlp_m, mlp_v;
     DevBuf act, dz, loss, io_a, io_b;
+    DevBuf mlp_tc, status;  // BF16 weights in tcgen05 core-matrix order; query status word
     uint32_t step = 0;
-    int infer_blocks = 0;
+    int infer_blocks = 0, tc_blocks = 0;
 };
 
 namespace {
@@ -439,6 +637,7 @@ cudaError_t nrc_refresh_copies(gbrt_nrc* r, cudaStream_t st) {
     const uint32_t n = std::max<uint32_t>(r->nentries, kNrcMlpParams);
     nrc_copy_kernel<<<(n + 255) / 256, 256, 0, st>>>(r->grid_w.as<float>(), r->nentries, r->grid_h.as<__half2>(),
                                                      r->mlp_w.as<float>(), r->mlp_h.as<__nv_bfloat16>());
+    nrc_tc_weights_kernel<<<(kTcWElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_tc.as<__nv_bfloat16>());
     return cudaGetLastError();
 }
 
@@ -479,6 +678,7 @@ cudaError_t nrc_adam(gbrt_nrc* r, cudaStream_t st) {
     nrc_adam_mlp_kernel<<<(kNrcMlpParams + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_g.as<float>(),
                                                                      r->mlp_m.as<float>(), r->mlp_v.as<float>(), a,
                                                                      r->mlp_h.as<__nv_bfloat16>());
+    nrc_tc_weights_kernel<<<(kTcWElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_tc.as<__nv_bfloat16>());
     return cudaGetLastError();
 }
 
@@ -500,6 +700,11 @@ cudaError_t nrc_kernel_setup(gbrt_nrc* r) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, nrc_infer_kernel, 128, kInferSmem);
         r->infer_blocks = sms * std::max(per, 1);
+        e = cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        if (e != cudaSuccess) return e;
+        int per_tc = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_tc, nrc_infer_tc_kernel, 128, kTcSmem);
+        r->tc_blocks = sms * std::max(std::min(per_tc, 4), 1);  // 4 x 64 tensor-memory columns per SM at most
     }
     return cudaSuccess;
 }
@@ -509,6 +714,12 @@ cudaError_t nrc_query_device(gbrt_nrc* r, const float4* q, uint32_t n, float4* o
     if (n == 0) return cudaSuccess;
     cudaError_t e = nrc_kernel_setup(r);
     if (e != cudaSuccess) return e;
+    if (!(r->cfg.flags & GBRT_NRC_QUERY_MMA_SYNC)) {
+        const uint32_t need = (n + kTcRows - 1) / kTcRows;
+        nrc_infer_tc_kernel<<<std::min<uint32_t>(need, (uint32_t)r->tc_blocks), 128, kTcSmem, st>>>(
+            r->view, q, n, out, nullptr, r->mlp_tc.as<__nv_bfloat16>(), r->status.as<uint32_t>());
+        return cudaGetLastError();
+    }
     const uint32_t need = (n + kInferWarps * 32 - 1) / (kInferWarps * 32);
     nrc_infer_kernel<<<std::min<uint32_t>(need, (uint32_t)r->infer_blocks), 128, kInferSmem, st>>>(r->view, q, n, out,
                                                                                                    nullptr);
@@ -519,7 +730,12 @@ cudaError_t nrc_query_counted(gbrt_nrc* r, const float4* q, const uint32_t* n_de
                               cudaStream_t st) {
     cudaError_t e = nrc_kernel_setup(r);
     if (e != cudaSuccess) return e;
-    nrc_infer_kernel<<<r->infer_blocks, 128, kInferSmem, st>>>(r->view, q, n_max, out, n_dev);
+    if (!(r->cfg.flags & GBRT_NRC_QUERY_MMA_SYNC))
+        nrc_infer_tc_kernel<<<r->tc_blocks, 128, kTcSmem, st>>>(r->view, q, n_max, out, n_dev,
+                                                                r->mlp_tc.as<__nv_bfloat16>(),
+                                                                r->status.as<uint32_t>());
+    else
+        nrc_infer_kernel<<<r->infer_blocks, 128, kInferSmem, st>>>(r->view, q, n_max, out, n_dev);
     return cudaGetLastError();
 }
 
@@ -561,6 +777,8 @@ int gbrt_nrc_create(gbrt_ctx* c, const gbrt_nrc_config* cfg, gbrt_nrc** out) {
     for (DevBuf* b : {&r->mlp_w, &r->mlp_g, &r->mlp_m, &r->mlp_v})
         if (e == cudaSuccess) e = b->alloc(kNrcMlpParams * 4);
     if (e == cudaSuccess) e = r->mlp_h.alloc(kBf16Padded * 2);
+    if (e == cudaSuccess) e = r->mlp_tc.alloc(kTcWElems * 2);
+    if (e == cudaSuccess) e = r->status.alloc(4);
     if (e == cudaSuccess) e = r->loss.alloc(4);
     if (e != cudaSuccess) {
         delete r;
@@ -583,6 +801,7 @@ int gbrt_nrc_create(gbrt_ctx* c, const gbrt_nrc_config* cfg, gbrt_nrc** out) {
     for (DevBuf* b : {&r->grid_m, &r->grid_v, &r->mlp_m, &r->mlp_v})
         if (e == cudaSuccess) e = cudaMemsetAsync(b->p, 0, b->bytes, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(r->mlp_h.p, 0, r->mlp_h.bytes, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->status.p, 0, 4, st);
     if (e == cudaSuccess) e = nrc_refresh_copies(r, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
@@ -626,7 +845,10 @@ int gbrt_nrc_query(gbrt_nrc* r, const float* pos4, uint32_t n, float* out4) {
     CU(c, cudaMemcpyAsync(r->io_a.p, pos4, (size_t)n * 16, cudaMemcpyHostToDevice, st), "upload");
     CU(c, nrc_query_device(r, r->io_a.as<float4>(), n, r->io_b.as<float4>(), st), "query");
     CU(c, cudaMemcpyAsync(out4, r->io_b.p, (size_t)n * 16, cudaMemcpyDeviceToHost, st), "download");
+    uint32_t status = 0;
+    CU(c, cudaMemcpyAsync(&status, r->status.p, 4, cudaMemcpyDeviceToHost, st), "download");
     CU(c, cudaStreamSynchronize(st), "sync");
+    if (status) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
     return GBRT_OK;
 }
 
@@ -724,11 +946,14 @@ extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, 
     if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
     DeviceCounters dc;
     CU(c, cudaMemcpyAsync(&dc, out.counters, sizeof(dc), cudaMemcpyDeviceToHost, st), "download counters");
+    uint32_t qstatus = 0;
+    CU(c, cudaMemcpyAsync(&qstatus, r->status.p, 4, cudaMemcpyDeviceToHost, st), "download");
     CU(c, cudaStreamSynchronize(st), "render");
     float ms = 0.0f;
     CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
     fill_stats(stats, dc, ms, 0);
     if (loss) *loss = lsum;
     if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit");
+    if (qstatus) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
     return GBRT_OK;
 }

@@ -202,7 +202,10 @@ class Job:
 class NrcConfig(C.Structure):
     _fields_ = [("log2_table", C.c_uint32), ("base_resolution", C.c_uint32), ("growth", C.c_float),
                 ("learning_rate", C.c_float), ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("flags", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+NRC_QUERY_MMA_SYNC = 0x1
 
 
 class NrcRenderOpts(C.Structure):
@@ -215,10 +218,10 @@ class Nrc:
     MLP_PARAMS = 18624
 
     def __init__(self, ctx, box_lo, box_hi, log2_table=19, base_resolution=16, growth=1.447, learning_rate=1e-2,
-                 seed=1):
+                 seed=1, flags=0):
         self.ctx = ctx
         self.cfg = NrcConfig(log2_table, base_resolution, growth, learning_rate, (C.c_float * 3)(*box_lo),
-                             (C.c_float * 3)(*box_hi), seed)
+                             (C.c_float * 3)(*box_hi), seed, flags, 0)
         h = P()
         ctx.check(ctx.L.gbrt_nrc_create(ctx.h, C.byref(self.cfg), C.byref(h)))
         self.h = h
