@@ -47,6 +47,44 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+NRC_MLP_FLOPS = 2 * (32 * 64 + 4 * 64 * 64 + 64 * 3)  # per query: 32 -> 64 x5 -> 3, no bias
+
+
+def nrc_mlp_rate(ctx, lo, hi, n=1 << 24, reps=10):
+    """Device time of cache queries (hash-grid encoding + MLP) over n seeded
+    positions in the box, for the tcgen05 and the mma.sync kernel, as MLP
+    TFLOP/s against the bf16 peak.  n float4 in and out = 512 MiB, above L2."""
+    import torch
+    from rustracer_gb300 import gbrt
+    g = torch.Generator(device="cuda").manual_seed(7)
+    pos = torch.zeros(n, 4, device="cuda")
+    lo_t, hi_t = torch.tensor(lo, device="cuda"), torch.tensor(hi, device="cuda")
+    pos[:, :3] = lo_t + torch.rand(n, 3, device="cuda", generator=g) * (hi_t - lo_t)
+    out = torch.empty_like(pos)
+    torch.cuda.synchronize()
+    peak, how = measured_bf16_tflops()
+    res = {"queries": n, "flop_per_query": NRC_MLP_FLOPS, "peak_tflops": peak, "peak_kind": how,
+           "note": "a query is 128 gathers from the FP16 hash table (16 levels x 8 corners) before 18,624 MACs; "
+                   "the table gathers bound it, not the tensor pipe"}
+    for name, flags in (("tcgen05", 0), ("mma_sync", gbrt.NRC_QUERY_MMA_SYNC)):
+        c = gbrt.Nrc(ctx, lo, hi, log2_table=19, flags=flags)
+        for _ in range(3):
+            c.query_device(pos.data_ptr(), n, out.data_ptr())
+        ms = sorted(c.query_device(pos.data_ptr(), n, out.data_ptr()) for _ in range(reps))[reps // 2]
+        tf = n * NRC_MLP_FLOPS / (ms * 1e-3) / 1e12
+        res[name] = {"device_ms": round(ms, 3), "mlp_tflops": round(tf, 2), "frac": round(tf / peak, 4),
+                     "mqueries_per_s": round(n / ms / 1e3, 1)}
+        c.close()
+    return res
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while
     the timed region runs."""
@@ -527,6 +565,7 @@ def run_nrc(args):
     with ClockSampler(0) as clk:
         t_pt, pts_pt, rays_pt, tot_pt = curve(pt_step, args.max_frames)
         t_nrc, pts_nrc, rays_nrc, tot_nrc = curve(nrc_step, 4 * args.max_frames)
+        mlp = nrc_mlp_rate(ctx, tuple(map(float, lo)), tuple(map(float, hi)))
     clocks = clk.summary()
     line = {"metric": "time to relMSE <= 1e-2", "value": None if t_nrc is None else t_nrc / 1e3, "unit": "s",
             "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": tot_nrc, "higher_is_better": False,
@@ -546,6 +585,7 @@ def run_nrc(args):
                       "curve": pts_nrc[:: max(1, len(pts_nrc) // 24)], "mrays_per_s": rays_nrc / tot_nrc / 1e3,
                       "final_loss": losses[-1] if losses else None},
             "speedup": (t_pt / t_nrc) if (t_pt and t_nrc) else None,
+            "mlp": mlp,
             "clocks": clocks}
     print(json.dumps(line), flush=True)
 

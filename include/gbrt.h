@@ -538,6 +538,11 @@ int gbrt_nrc_destroy(gbrt_nrc* nrc);
 int gbrt_nrc_params(gbrt_nrc* nrc, float* mlp, float* grid, int upload);
 /* n queries: pos4 = (x, y, z, payload) per query, out4 = (r, g, b, payload). */
 int gbrt_nrc_query(gbrt_nrc* nrc, const float* pos4, uint32_t n, float* out4);
+/* The same with device buffers (n float4 each, 16-byte aligned, on the
+ * context's device, e.g. framework tensors): runs on the context stream,
+ * waits for it, and returns the query kernel's device time in *device_ms
+ * (may be NULL). */
+int gbrt_nrc_query_device(gbrt_nrc* nrc, const float* pos4_dev, uint32_t n, float* out4_dev, float* device_ms);
 /* Loss and gradients of one batch (pos4, target4 = (r, g, b, -)); step != 0
  * then applies one Adam step.  loss / grad_mlp / grad_grid may be NULL. */
 int gbrt_nrc_train(gbrt_nrc* nrc, const float* pos4, const float* target4, uint32_t n, int step, float* loss,

@@ -702,9 +702,16 @@ cudaError_t nrc_kernel_setup(gbrt_nrc* r) {
         r->infer_blocks = sms * std::max(per, 1);
         e = cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         if (e != cudaSuccess) return e;
-        int per_tc = 0;
+        cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        // CTAs per SM by shared memory (the occupancy query has reported 1 for this
+        // kernel where the launch fits 4), at most 4 x 64 tensor-memory columns
+        int smem_sm = 0, smem_rsv = 0, per_tc = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_tc, nrc_infer_tc_kernel, 128, kTcSmem);
-        r->tc_blocks = sms * std::max(std::min(per_tc, 4), 1);  // 4 x 64 tensor-memory columns per SM at most
+        per_tc = std::max(per_tc, smem_sm / (int)(kTcSmem + (size_t)smem_rsv));
+        r->tc_blocks = sms * std::max(std::min(per_tc, 4), 1);
     }
     return cudaSuccess;
 }
@@ -848,6 +855,25 @@ int gbrt_nrc_query(gbrt_nrc* r, const float* pos4, uint32_t n, float* out4) {
     uint32_t status = 0;
     CU(c, cudaMemcpyAsync(&status, r->status.p, 4, cudaMemcpyDeviceToHost, st), "download");
     CU(c, cudaStreamSynchronize(st), "sync");
+    if (status) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
+    return GBRT_OK;
+}
+
+int gbrt_nrc_query_device(gbrt_nrc* r, const float* pos4_dev, uint32_t n, float* out4_dev, float* device_ms) {
+    if (!r) return GBRT_E_INVALID;
+    gbrt_ctx* c = r->ctx;
+    if (n && (!pos4_dev || !out4_dev)) return fail(c, GBRT_E_INVALID, "NULL argument");
+    if (((uintptr_t)pos4_dev | (uintptr_t)out4_dev) & 15u) return fail(c, GBRT_E_INVALID, "buffers must be 16-byte aligned");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CU(c, cudaEventRecord(c->ev0, st), "event");
+    if (n) CU(c, nrc_query_device(r, reinterpret_cast<const float4*>(pos4_dev), n, reinterpret_cast<float4*>(out4_dev), st),
+              "query");
+    CU(c, cudaEventRecord(c->ev1, st), "event");
+    uint32_t status = 0;
+    CU(c, cudaMemcpyAsync(&status, r->status.p, 4, cudaMemcpyDeviceToHost, st), "download");
+    CU(c, cudaStreamSynchronize(st), "sync");
+    if (device_ms) CU(c, cudaEventElapsedTime(device_ms, c->ev0, c->ev1), "event time");
     if (status) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
     return GBRT_OK;
 }

@@ -66,6 +66,7 @@ SIGNATURES = {
     "gbrt_nrc_destroy": (i32, [P]),
     "gbrt_nrc_params": (i32, [P, P, P, i32]),
     "gbrt_nrc_query": (i32, [P, P, u32, P]),
+    "gbrt_nrc_query_device": (i32, [P, P, u32, P, P]),
     "gbrt_nrc_train": (i32, [P, P, P, u32, i32, P, P, P]),
     "gbrt_render_nrc": (i32, [P, P, P, P, P, P, P, P]),
     "gbrt_scene_autotune": (i32, [P, P, u32, u32, P]),
@@ -245,6 +246,13 @@ class Nrc:
         out = np.zeros_like(q)
         self.ctx.check(self.ctx.L.gbrt_nrc_query(self.h, _p(q), len(q), _p(out)))
         return out[:, :3]
+
+    def query_device(self, pos4_ptr, n, out4_ptr):
+        """Queries on device buffers of n float4 (e.g. tensor.data_ptr()); returns the device ms."""
+        ms = C.c_float(0)
+        self.ctx.check(self.ctx.L.gbrt_nrc_query_device(self.h, C.c_void_p(pos4_ptr), n, C.c_void_p(out4_ptr),
+                                                        C.byref(ms)))
+        return ms.value
 
     def train(self, pos, target, step=True, grads=False):
         q = np.zeros((len(pos), 4), np.float32)

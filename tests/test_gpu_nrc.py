@@ -216,3 +216,21 @@ def test_render_with_cache_converges(gpu_ctx):
     e_c, e_p = _relmse(img_c, ref), _relmse(img_p, ref)
     assert e_c < e_p, (e_c, e_p, losses[:3], losses[-3:])
     assert np.mean(losses[-10:]) < np.mean(losses[:5]) / 10
+
+
+def test_query_device_buffers(gpu_ctx):
+    """gbrt_nrc_query_device on framework tensors gives the host-buffer query's result."""
+    import torch
+    rng = np.random.default_rng(13)
+    c = _cache(gpu_ctx)
+    mlp, grid = _random_params(rng)
+    c.set_params(mlp, grid)
+    pos = _points(rng, 3001)
+    y = c.query(pos)
+    p4 = torch.zeros(len(pos), 4, device="cuda")
+    p4[:, :3] = torch.from_numpy(pos).cuda()
+    out = torch.empty_like(p4)
+    torch.cuda.synchronize()
+    ms = c.query_device(p4.data_ptr(), len(pos), out.data_ptr())
+    assert ms >= 0.0
+    np.testing.assert_array_equal(out[:, :3].cpu().numpy(), y)
