@@ -466,7 +466,14 @@ int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t w
  * GBRT_E_BUSY, and a scene or accumulation buffer used by an unfinished job
  * cannot be destroyed or reset.  A skinned scene is animated by jobs that
  * carry skins: the scheduler admits such a job once no active job uses that
- * scene, then skins it and rebuilds its BVH before the job's first wave. */
+ * scene, then skins it and rebuilds its BVH before the job's first wave.
+ *
+ * A job may carry a radiance cache (cache != NULL): it is then rendered in
+ * waves of its own, exactly as gbrt_render_nrc renders the frame, followed
+ * by its training steps, and its image is bit-identical to that call's on a
+ * cache in the same state.  Jobs that share a cache train it in turn, in
+ * the order the scheduler runs them.  The cache calls (query, train,
+ * params, destroy) return GBRT_E_BUSY while the context has unfinished jobs. */
 #define GBRT_JOB_QUEUED   0u
 #define GBRT_JOB_RUNNING  1u
 #define GBRT_JOB_DONE     2u
@@ -481,6 +488,8 @@ typedef struct gbrt_job_desc {
     const gbrt_skin_raw* skins;   /* non-NULL: skin the scene (copied at submit) before the job */
     uint32_t nskin;
     uint32_t flags;               /* reserved, 0 */
+    struct gbrt_nrc* cache;       /* non-NULL: render with this radiance cache (gbrt_render_nrc) */
+    const struct gbrt_nrc_render_opts* cache_opts;  /* with cache: copied at submit */
 } gbrt_job_desc;
 
 typedef struct gbrt_job_info {

@@ -147,6 +147,14 @@ cudaError_t nrc_query_counted(gbrt_nrc* r, const float4* q, const uint32_t* n_de
                               cudaStream_t st);
 cudaError_t nrc_train_device(gbrt_nrc* r, const float4* pos, const float4* target, uint32_t n, cudaStream_t st);
 const gbrt::NrcView& nrc_view(const gbrt_nrc* r);
+// One frame rendered with the cache into out, then its training steps
+// (gbrt_render_nrc without the host copies); *what names a failed step.
+cudaError_t nrc_frame(gbrt_nrc* r, const DevScene& view, const gbrt_ubo& ubo, const gbrt::RenderOut& out,
+                      const WfState& wf, const gbrt_nrc_render_opts& opts, cudaStream_t st, float* loss,
+                      const char** what);
+// The cache's query status word (0: no tensor-core wait has timed out); waits for st.
+uint32_t nrc_status(gbrt_nrc* r, cudaStream_t st);
+gbrt_ctx* nrc_ctx(const gbrt_nrc* r);
 
 // jobs.cu: stops the scheduler thread after the queued jobs (ctx destroy).
 void jobs_shutdown(gbrt_ctx* c);

@@ -76,6 +76,8 @@ struct Job {
     uint8_t* out_rgba8 = nullptr;
     std::vector<gbrt_skin_raw> skins;
     bool has_skins = false;
+    gbrt_nrc* cache = nullptr;  // rendered alone through the cache (nrc_frame)
+    gbrt_nrc_render_opts copts{};
     // progress
     uint32_t npix = 0, ns = 0, sbase = 0, chunk = 0;
     uint32_t px0 = 0, s0 = 0;
@@ -118,6 +120,8 @@ struct JobQueue {
     void run();
     bool admit_one(std::unique_lock<std::mutex>& lk);
     int pack_and_launch();
+    int run_cache_job(Job* j, std::unique_lock<std::mutex>& lk);
+    int launch_next(std::unique_lock<std::mutex>& lk);
     void retire(Wave& w);
     void fail_active(int code, const std::string& msg);
 };
@@ -195,7 +199,7 @@ bool JobQueue::admit_one(std::unique_lock<std::mutex>& lk) {
 int JobQueue::pack_and_launch() {
     std::vector<Job*> order;
     for (Job* j : active)
-        if (j->paths_left) order.push_back(j);
+        if (j->paths_left && !j->cache) order.push_back(j);
     if (order.empty()) return 1;
     if (policy == GBRT_JOB_POLICY_SRPT)
         std::stable_sort(order.begin(), order.end(),
@@ -287,6 +291,70 @@ int JobQueue::pack_and_launch() {
     return GBRT_OK;
 }
 
+// Renders a cache job's whole frame and its training on the context stream
+// (lock released meanwhile; one host wait, for the training sample count),
+// then queues its completion like a wave's.  Called with the lock held.
+int JobQueue::run_cache_job(Job* j, std::unique_lock<std::mutex>& lk) {
+    j->paths_left = 0;
+    RenderOut out{};
+    out.width = j->acc->w;
+    out.height = j->acc->h;
+    out.accum = j->acc->buf.as<float4>();
+    out.rgba8 = j->out_rgba8 ? j->img.as<uchar4>() : nullptr;
+    out.counters = j->counters.as<DeviceCounters>();
+    WfState wf = ctx->wf;
+    wf.frame_sum = j->frame_sum.as<float4>();
+    const char* what = "";
+    lk.unlock();
+    cudaError_t e = nrc_frame(j->cache, j->scene->view, j->ubo, out, wf, j->copts, ctx->stream, nullptr, &what);
+    const uint32_t qstatus = e == cudaSuccess ? nrc_status(j->cache, ctx->stream) : 0u;
+    lk.lock();
+    if (e == cudaSuccess && qstatus) {
+        active.erase(std::find(active.begin(), active.end(), j));
+        finish_job(*this, j, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
+        cv_done.notify_all();
+        return GBRT_OK;
+    }
+    Wave wv;
+    if (e == cudaSuccess && free_events.empty()) {
+        cudaEvent_t ev;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) free_events.push_back(ev);
+    }
+    if (e == cudaSuccess) {
+        wv.ev = free_events.back();
+        free_events.pop_back();
+        e = cudaEventRecord(wv.ev, ctx->stream);
+        if (e != cudaSuccess) free_events.push_back(wv.ev);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail_active(GBRT_E_CUDA, std::string("cache job (") + what + "): " + cudaGetErrorString(e));
+        return GBRT_E_CUDA;
+    }
+    wv.finishing.push_back(j);
+    inflight.push_back(std::move(wv));
+    return GBRT_OK;
+}
+
+// Launches the next unit of work: a cache job when one comes first in the
+// policy's order, else a batched wave of the other jobs.  Returns GBRT_OK,
+// or 1 when no active job has paths left.  Lock held.
+int JobQueue::launch_next(std::unique_lock<std::mutex>& lk) {
+    Job* first = nullptr;
+    for (Job* j : active) {
+        if (!j->paths_left) continue;
+        const bool before = !first || (policy == GBRT_JOB_POLICY_SRPT
+                                           ? (j->paths_left < first->paths_left ||
+                                              (j->paths_left == first->paths_left && j->id < first->id))
+                                           : j->id < first->id);
+        if (before) first = j;
+    }
+    if (!first) return 1;
+    if (first->cache) return run_cache_job(first, lk);
+    return pack_and_launch();
+}
+
 // A wave's event has fired: finish the jobs it completed.  Lock held.
 void JobQueue::retire(Wave& w) {
     for (Job* j : w.finishing) {
@@ -333,7 +401,7 @@ void JobQueue::run() {
             inflight.pop_front();
             retire(w);
         }
-        if ((int)inflight.size() < kMaxInFlight && pack_and_launch() == GBRT_OK) continue;
+        if ((int)inflight.size() < kMaxInFlight && launch_next(lk) == GBRT_OK) continue;
         if (!inflight.empty()) {
             cudaEvent_t ev = inflight.front().ev;
             lk.unlock();
@@ -433,6 +501,8 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
         return fail(c, GBRT_E_INVALID, "need 0 < number_of_samples <= total_number_of_samples");
     if (u.number_of_bounces > 31) return fail(c, GBRT_E_INVALID, "jobs trace at most 31 bounces");
     if (d->skins && d->nskin == 0) return fail(c, GBRT_E_INVALID, "skins given with nskin = 0");
+    if (d->cache && (!d->cache_opts || nrc_ctx(d->cache) != c))
+        return fail(c, GBRT_E_INVALID, "a cache job needs cache_opts and a cache of this context");
     const uint64_t npix = (uint64_t)d->accum->w * d->accum->h;
     if (npix > kWaveCap) return fail(c, GBRT_E_INVALID, "job image larger than " + std::to_string(kWaveCap) + " pixels");
     auto j = std::make_unique<Job>();
@@ -443,6 +513,10 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
     if (d->skins) {
         j->skins.assign(d->skins, d->skins + d->nskin);
         j->has_skins = true;
+    }
+    if (d->cache) {
+        j->cache = d->cache;
+        j->copts = *d->cache_opts;
     }
     j->npix = (uint32_t)npix;
     j->ns = u.number_of_samples;

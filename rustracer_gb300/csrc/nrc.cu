@@ -595,6 +595,7 @@ __global__ void nrc_copy_kernel(const float* grid_w, uint32_t ngrid2, __half2* g
 using gbrt_host::DevBuf;
 using gbrt_host::DeviceGuard;
 using gbrt_host::fail;
+using gbrt_host::jobs_outstanding;
 
 struct gbrt_nrc {
     gbrt_ctx* ctx = nullptr;
@@ -821,6 +822,7 @@ int gbrt_nrc_create(gbrt_ctx* c, const gbrt_nrc_config* cfg, gbrt_nrc** out) {
 
 int gbrt_nrc_destroy(gbrt_nrc* r) {
     if (!r) return GBRT_OK;
+    if (jobs_outstanding(r->ctx)) return fail(r->ctx, GBRT_E_BUSY, "jobs are running on this context");
     DeviceGuard g(r->ctx->device);
     cudaStreamSynchronize(r->ctx->stream);
     delete r;
@@ -830,6 +832,7 @@ int gbrt_nrc_destroy(gbrt_nrc* r) {
 int gbrt_nrc_params(gbrt_nrc* r, float* mlp, float* grid, int upload) {
     if (!r) return GBRT_E_INVALID;
     gbrt_ctx* c = r->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
     const size_t ng = (size_t)r->nentries * 2 * 4;
@@ -844,6 +847,7 @@ int gbrt_nrc_params(gbrt_nrc* r, float* mlp, float* grid, int upload) {
 int gbrt_nrc_query(gbrt_nrc* r, const float* pos4, uint32_t n, float* out4) {
     if (!r) return GBRT_E_INVALID;
     gbrt_ctx* c = r->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && (!pos4 || !out4)) return fail(c, GBRT_E_INVALID, "NULL argument");
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
@@ -862,6 +866,7 @@ int gbrt_nrc_query(gbrt_nrc* r, const float* pos4, uint32_t n, float* out4) {
 int gbrt_nrc_query_device(gbrt_nrc* r, const float* pos4_dev, uint32_t n, float* out4_dev, float* device_ms) {
     if (!r) return GBRT_E_INVALID;
     gbrt_ctx* c = r->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && (!pos4_dev || !out4_dev)) return fail(c, GBRT_E_INVALID, "NULL argument");
     if (((uintptr_t)pos4_dev | (uintptr_t)out4_dev) & 15u) return fail(c, GBRT_E_INVALID, "buffers must be 16-byte aligned");
     DeviceGuard g(c->device);
@@ -882,6 +887,7 @@ int gbrt_nrc_train(gbrt_nrc* r, const float* pos4, const float* target4, uint32_
                    float* grad_mlp, float* grad_grid) {
     if (!r) return GBRT_E_INVALID;
     gbrt_ctx* c = r->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n == 0 || !pos4 || !target4) return fail(c, GBRT_E_INVALID, "empty batch or NULL argument");
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
@@ -902,6 +908,79 @@ int gbrt_nrc_train(gbrt_nrc* r, const float* pos4, const float* target4, uint32_
 
 }  // extern "C"
 
+namespace gbrt_host {
+
+// One frame with the cache on stream st: traces into out (its accumulation,
+// image and counters) with the wavefront buffers of wf (frame_sum sized for
+// out, cap paths per wave), then runs opts.train_steps Adam steps on the
+// frame's training samples.  Host-synchronises once, for the number of
+// training samples.  *what names the failed step.
+cudaError_t nrc_frame(gbrt_nrc* r, const DevScene& view, const gbrt_ubo& ubo, const RenderOut& out, const WfState& wf,
+                      const gbrt_nrc_render_opts& opts, cudaStream_t st, float* loss, const char** what) {
+    const uint64_t paths = (uint64_t)out.width * out.height * ubo.number_of_samples;
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(paths, wf.cap), kMaxWavePaths);
+    const uint32_t tmax = std::max<uint32_t>(opts.train_samples, 1u) * 2u;  // room for the hash's spread
+    cudaError_t e = cudaSuccess;
+    *what = "cudaMalloc(cache frame buffers)";
+    if (r->f_cap < cap) {
+        for (DevBuf* b : {&r->f_query, &r->f_qout, &r->f_snap_pos, &r->f_snap_rad, &r->f_snap_tp})
+            if ((e = b->alloc((size_t)cap * sizeof(float4))) != cudaSuccess) return e;
+        r->f_cap = cap;
+    }
+    if (r->f_train_max < tmax) {
+        if ((e = r->f_train_pos.alloc((size_t)tmax * sizeof(float4))) != cudaSuccess) return e;
+        if ((e = r->f_train_tgt.alloc((size_t)tmax * sizeof(float4))) != cudaSuccess) return e;
+        r->f_train_max = tmax;
+    }
+    if ((e = r->f_counts.reserve(64 * sizeof(uint32_t))) != cudaSuccess) return e;
+    NrcWave nw{};
+    nw.query = r->f_query.as<float4>();
+    nw.qout = r->f_qout.as<float4>();
+    nw.snap_pos = r->f_snap_pos.as<float4>();
+    nw.snap_rad = r->f_snap_rad.as<float4>();
+    nw.snap_tp = r->f_snap_tp.as<float4>();
+    nw.train_pos = r->f_train_pos.as<float4>();
+    nw.train_tgt = r->f_train_tgt.as<float4>();
+    nw.counts = r->f_counts.as<uint32_t>();
+    nw.train_max = r->f_train_max;
+    const double frac = std::min(1.0, (double)opts.train_samples / (double)paths);
+    nw.train_thresh = (uint32_t)std::min(65536.0, std::ceil(frac * 65536.0));
+    nw.min_roughness = opts.min_roughness;
+    nw.disabled = opts.disabled ? 1u : 0u;
+    WfState w = wf;
+    w.cap = cap;
+    *what = "wavefront launch";
+    if ((e = cudaMemsetAsync(nw.counts + 32, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+    if ((e = launch_wavefront(view, ubo, out, w, st, nullptr, &nw, r)) != cudaSuccess) return e;
+    uint32_t ntrain = 0;
+    *what = "training sample count";
+    if ((e = cudaMemcpyAsync(&ntrain, nw.counts + 32, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    ntrain = std::min(ntrain, nw.train_max);
+    *what = "cache training";
+    for (uint32_t k = 0; k < opts.train_steps && ntrain > 0; ++k)
+        if ((e = nrc_train_device(r, nw.train_pos, nw.train_tgt, ntrain, st)) != cudaSuccess) return e;
+    if (loss) {
+        *loss = 0.0f;  // loss of the last step
+        if (ntrain > 0 && opts.train_steps)
+            if ((e = cudaMemcpyAsync(loss, r->loss.p, 4, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    }
+    *what = "";
+    return cudaSuccess;
+}
+
+uint32_t nrc_status(gbrt_nrc* r, cudaStream_t st) {
+    uint32_t v = 0;
+    if (cudaMemcpyAsync(&v, r->status.p, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ~0u;
+    return v;
+}
+
+gbrt_ctx* nrc_ctx(const gbrt_nrc* r) { return r->ctx; }
+
+}  // namespace gbrt_host
+
 extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t* out_rgba8,
                                gbrt_stats* stats, const gbrt_nrc_render_opts* opts, float* loss) {
     using namespace gbrt_host;
@@ -921,32 +1000,6 @@ extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, 
     const uint64_t paths = (uint64_t)npix * ns;
     const uint32_t cap = (uint32_t)std::min<uint64_t>(paths, kMaxWavePaths);
     CU(c, wavefront_reserve(c, cap, npix), "cudaMalloc(wavefront buffers)");
-    const uint32_t tmax = std::max<uint32_t>(opts->train_samples, 1u) * 2u;  // room for the hash's spread
-    if (r->f_cap < cap) {
-        for (DevBuf* b : {&r->f_query, &r->f_qout, &r->f_snap_pos, &r->f_snap_rad, &r->f_snap_tp})
-            CU(c, b->alloc((size_t)cap * sizeof(float4)), "cudaMalloc(cache frame buffers)");
-        r->f_cap = cap;
-    }
-    if (r->f_train_max < tmax) {
-        CU(c, r->f_train_pos.alloc((size_t)tmax * sizeof(float4)), "cudaMalloc(training buffers)");
-        CU(c, r->f_train_tgt.alloc((size_t)tmax * sizeof(float4)), "cudaMalloc(training buffers)");
-        r->f_train_max = tmax;
-    }
-    CU(c, r->f_counts.reserve(64 * sizeof(uint32_t)), "cudaMalloc(counters)");
-    NrcWave nw{};
-    nw.query = r->f_query.as<float4>();
-    nw.qout = r->f_qout.as<float4>();
-    nw.snap_pos = r->f_snap_pos.as<float4>();
-    nw.snap_rad = r->f_snap_rad.as<float4>();
-    nw.snap_tp = r->f_snap_tp.as<float4>();
-    nw.train_pos = r->f_train_pos.as<float4>();
-    nw.train_tgt = r->f_train_tgt.as<float4>();
-    nw.counts = r->f_counts.as<uint32_t>();
-    nw.train_max = r->f_train_max;
-    const double frac = std::min(1.0, (double)opts->train_samples / (double)paths);
-    nw.train_thresh = (uint32_t)std::min(65536.0, std::ceil(frac * 65536.0));
-    nw.min_roughness = opts->min_roughness;
-    nw.disabled = opts->disabled ? 1u : 0u;
     RenderOut out{};
     out.width = W;
     out.height = H;
@@ -957,29 +1010,20 @@ extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, 
         out.rgba8 = c->scratch_img.as<uchar4>();
     }
     CU(c, cudaMemsetAsync(out.counters, 0, sizeof(DeviceCounters), st), "memset");
-    CU(c, cudaMemsetAsync(nw.counts + 32, 0, sizeof(uint32_t), st), "memset");
     CU(c, cudaEventRecord(c->ev0, st), "event");
-    CU(c, launch_wavefront(s->view, *ubo, out, c->wf, st, nullptr, &nw, r), "wavefront launch");
-    uint32_t ntrain = 0;
-    CU(c, cudaMemcpyAsync(&ntrain, nw.counts + 32, 4, cudaMemcpyDeviceToHost, st), "download");
-    CU(c, cudaStreamSynchronize(st), "render");
-    ntrain = std::min(ntrain, nw.train_max);
-    for (uint32_t k = 0; k < opts->train_steps && ntrain > 0; ++k)
-        CU(c, nrc_train_device(r, nw.train_pos, nw.train_tgt, ntrain, st), "cache training");
-    float lsum = 0.0f;  // loss of the last step
-    if (ntrain > 0 && opts->train_steps) CU(c, cudaMemcpyAsync(&lsum, r->loss.p, 4, cudaMemcpyDeviceToHost, st), "download");
+    float lsum = 0.0f;
+    const char* what = "";
+    CU(c, nrc_frame(r, s->view, *ubo, out, c->wf, *opts, st, &lsum, &what), what);
     CU(c, cudaEventRecord(c->ev1, st), "event");
     if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
     DeviceCounters dc;
     CU(c, cudaMemcpyAsync(&dc, out.counters, sizeof(dc), cudaMemcpyDeviceToHost, st), "download counters");
-    uint32_t qstatus = 0;
-    CU(c, cudaMemcpyAsync(&qstatus, r->status.p, 4, cudaMemcpyDeviceToHost, st), "download");
     CU(c, cudaStreamSynchronize(st), "render");
     float ms = 0.0f;
     CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
     fill_stats(stats, dc, ms, 0);
     if (loss) *loss = lsum;
     if (dc.status) return fail(c, GBRT_E_DEVICE_LIMIT, "a kernel reported a traversal limit");
-    if (qstatus) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
+    if (nrc_status(r, st)) return fail(c, GBRT_E_DEVICE_LIMIT, "a tensor-core wait of the cache query timed out");
     return GBRT_OK;
 }

@@ -117,7 +117,8 @@ class RenderOpts(C.Structure):
 
 class JobDesc(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("ubo", C.c_void_p), ("accum", C.c_void_p), ("out_rgba8", C.c_void_p),
-                ("skins", C.c_void_p), ("nskin", C.c_uint32), ("flags", C.c_uint32)]
+                ("skins", C.c_void_p), ("nskin", C.c_uint32), ("flags", C.c_uint32), ("cache", C.c_void_p),
+                ("cache_opts", C.c_void_p)]
 
 
 class Context:
@@ -147,9 +148,12 @@ class Context:
     def jobs_configure(self, hbm_budget=0, policy=POLICY_SRPT):
         self.check(self.L.gbrt_jobs_configure(self.h, hbm_budget, policy))
 
-    def submit(self, scene, ubo, accum, image=True, skins=None):
-        """Queues one frame of `scene` into `accum`; returns a Job."""
-        return Job(self, scene, ubo, accum, image, skins)
+    def submit(self, scene, ubo, accum, image=True, skins=None, cache=None, min_roughness=0.0,
+               train_samples=1 << 16, train_steps=1):
+        """Queues one frame of `scene` into `accum` (through the radiance
+        cache `cache`, an Nrc, when given); returns a Job."""
+        return Job(self, scene, ubo, accum, image, skins, cache,
+                   None if cache is None else NrcRenderOpts(min_roughness, train_samples, train_steps, 0))
 
     def close(self):
         if getattr(self, "h", None):
@@ -164,15 +168,18 @@ class Job:
     """A submitted frame: ``wait()`` returns its info (state, status, queue
     and end-to-end latency in ms, stats) and fills ``image``."""
 
-    def __init__(self, ctx, scene, ubo, accum, image=True, skins=None):
+    def __init__(self, ctx, scene, ubo, accum, image=True, skins=None, cache=None, cache_opts=None):
         self.ctx = ctx
         self._ubo = np.asarray(ubo, T.UBO).reshape(())
         self.image = np.zeros((accum.h_, accum.w, 4), np.uint8) if image else None
         self._skins = None if skins is None else np.ascontiguousarray(skins, T.SKIN)
+        self._copts = cache_opts
         d = JobDesc(scene.h, self._ubo.ctypes.data, accum.h,
                     self.image.ctypes.data if image else None,
                     self._skins.ctypes.data if self._skins is not None else None,
-                    0 if self._skins is None else len(self._skins), 0)
+                    0 if self._skins is None else len(self._skins), 0,
+                    cache.h if cache is not None else None,
+                    C.addressof(cache_opts) if cache_opts is not None else None)
         jid = u64()
         ctx.check(ctx.L.gbrt_job_submit(ctx.h, C.byref(d), C.byref(jid)))
         self.id = jid.value

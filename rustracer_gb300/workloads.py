@@ -132,12 +132,14 @@ def serving_pool(max_subdiv=9):
 
 
 def serving_trace(seed=0, n=200, rate=200.0, nscenes=8, skinned=7, res_lo=256 * 256, res_hi=1920 * 1080,
-                  spp_lo=1, spp_hi=256):
+                  spp_lo=1, spp_hi=256, cache_frac=0.25):
     """n jobs: Poisson arrivals at `rate` per second; scene uniform over the
     pool; pixel count log-uniform in [res_lo, res_hi] at 16:9 (256^2 .. 1080p);
     spp log-uniform in [spp_lo, spp_hi]; jobs on the skinned scene carry an
-    animation time."""
+    animation time; a fraction cache_frac of the jobs (own stream, seed + 1)
+    render through their scene's radiance cache."""
     rng = np.random.default_rng(seed)
+    use_cache = np.random.default_rng(seed + 1).random(n) < cache_frac
     t = np.cumsum(rng.exponential(1.0 / rate, n))
     jobs = []
     for i in range(n):
@@ -147,7 +149,8 @@ def serving_trace(seed=0, n=200, rate=200.0, nscenes=8, skinned=7, res_lo=256 * 
         spp = int(round(math.exp(rng.uniform(math.log(spp_lo), math.log(spp_hi)))))
         k = int(rng.integers(nscenes))
         jobs.append(dict(arrival=float(t[i]), scene=k, width=w, height=h, spp=max(1, spp),
-                         anim_time=float(rng.uniform(0, 6.28)) if k == skinned else None))
+                         anim_time=float(rng.uniform(0, 6.28)) if k == skinned else None,
+                         cache=bool(use_cache[i])))
     return jobs
 
 
@@ -225,3 +228,18 @@ def city_scene(seed=0, n_boxes=2500, n_spheres=1500, sphere_subdiv=3, nmat=16):
                   camera=dict(eye=(0.0, 28.0, 60.0), direction=(0.0, -0.45, -1.0), fov_deg=55.0), name="city")
     sd.instanced_triangles = int(n_boxes * 12 + n_spheres * len(sf) + 2)
     return sd
+
+
+def world_box(sd, pad=0.5):
+    """Axis-aligned box around a scene's world-space geometry: the vertex
+    box's corners carried through every instance transform, padded."""
+    p = sd.vertices["pos"][:, :3].astype(np.float64)
+    lo, hi = p.min(0), p.max(0)
+    corners = np.array([[x, y, z, 1.0] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])])
+    if len(sd.instances):
+        m = sd.instances["transform"].reshape(-1, 3, 4).astype(np.float64)
+        w = np.einsum("nij,cj->nci", m, corners).reshape(-1, 3)
+    else:
+        w = corners[:, :3]
+    return tuple(map(float, w.min(0) - pad)), tuple(map(float, w.max(0) + pad))
+

@@ -115,3 +115,57 @@ def test_busy_while_jobs_outstanding(gpu_ctx):
     assert job.poll() is None or job.info["state"] == gbrt.JOB_DONE
     assert job.wait()["status"] == 0
     sc.render(sd.ubo(16, 16, samples=1), gbrt.Accum(gpu_ctx, 16, 16))  # usable again
+
+
+def test_cache_jobs_equal_render_nrc(gpu_ctx):
+    """Jobs carrying a radiance cache, submitted among plain jobs: a cache
+    job's accumulation and image are bit-identical to gbrt_render_nrc's on a
+    cache in the same state (a second cache given the same parameters), its
+    training steps run (the parameters move), and the plain jobs still equal
+    their solo renders."""
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=4)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    p = sd.vertices["pos"][:, :3]
+    lo, hi = tuple(map(float, p.min(0) - 0.05)), tuple(map(float, p.max(0) + 0.05))
+    ca = gbrt.Nrc(gpu_ctx, lo, hi, log2_table=16, learning_rate=1e-3)
+    cb = gbrt.Nrc(gpu_ctx, lo, hi, log2_table=16, learning_rate=1e-3, seed=99)
+    W, H = 160, 120
+    warm = sd.ubo(W, H, samples=1, total=1, bounces=8, exposure=1.0)
+    ca.render(sc, warm, gbrt.Accum(gpu_ctx, W, H), image=False, train_samples=4096, train_steps=4)
+    mlp, grid = ca.params()
+    cb.set_params(mlp, grid)
+    u = sd.ubo(W, H, samples=2, total=3, bounces=8, exposure=1.0)
+    acc_a = gbrt.Accum(gpu_ctx, W, H)
+    ref = ca.render(sc, u, acc_a, image=True, min_roughness=0.0, train_samples=4096, train_steps=2)
+    plain = [(sd.ubo(w, h, samples=s, bounces=6, exposure=1.0), w, h) for w, h, s in ((64, 48, 4), (320, 200, 2))]
+    solo = [_solo(gpu_ctx, sc, ub, w, h) for ub, w, h in plain]
+    acc_b = gbrt.Accum(gpu_ctx, W, H)
+    accs = [gbrt.Accum(gpu_ctx, w, h) for _, w, h in plain]
+    jobs = [gpu_ctx.submit(sc, plain[0][0], accs[0]),
+            gpu_ctx.submit(sc, u, acc_b, cache=cb, min_roughness=0.0, train_samples=4096, train_steps=2),
+            gpu_ctx.submit(sc, plain[1][0], accs[1])]
+    infos = [j.wait() for j in jobs]
+    assert all(i["status"] == 0 for i in infos)
+    assert np.array_equal(acc_b.download(), acc_a.download())
+    assert np.array_equal(jobs[1].image.reshape(ref["image"].shape), ref["image"])
+    assert infos[1]["stats"]["rays_camera"] == W * H * 2
+    for k, (img, acc_ref) in enumerate(solo):
+        assert np.array_equal(jobs[2 * k].image.reshape(img.shape), img)
+        assert np.array_equal(accs[k].download(), acc_ref)
+    m2, _ = cb.params()
+    assert not np.array_equal(m2, mlp)
+
+
+def test_cache_calls_busy_while_jobs_outstanding(gpu_ctx):
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=4)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    c = gbrt.Nrc(gpu_ctx, (-2.0, -2.0, -2.0), (2.0, 2.0, 2.0), log2_table=12)
+    acc = gbrt.Accum(gpu_ctx, 1280, 720)
+    job = gpu_ctx.submit(sc, sd.ubo(1280, 720, samples=32, bounces=8, exposure=1.0), acc, image=False)
+    with pytest.raises(gbrt.GbrtError) as e:
+        c.query(np.zeros((4, 3), np.float32))
+    assert e.value.code == gbrt.E_BUSY
+    assert job.wait()["status"] == 0
+    assert c.query(np.zeros((4, 3), np.float32)).shape == (4, 3)
