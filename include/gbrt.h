@@ -314,7 +314,7 @@ int gbrt_scene_destroy(gbrt_scene* scene);
  * per-primitive vkCmdBuildAccelerationStructuresKHR of create_as
  * (acceleration_structures.rs:17-76,79-111).
  *
- * flags: 0, or GBRT_BUILD_NO_FLATTEN.  By default the next gbrt_tlas_build
+ * flags: 0, or GBRT_BUILD_NO_FLATTEN and/or GBRT_BUILD_WIDTH4.  By default the next gbrt_tlas_build
  * flattens transformed instances into the world BVH when the flattened scene
  * has at most GBRT_FLATTEN_MAX_TRIANGLES triangles: their triangles are
  * transformed to world space once (row-major 3x4, each product and sum
@@ -323,6 +323,9 @@ int gbrt_scene_destroy(gbrt_scene* scene);
  * are transformed to object space instead.  The two give hits that can
  * differ in the last bits of t, u, v (the oracle follows the same rule). */
 #define GBRT_BUILD_NO_FLATTEN 0x1u
+/* GBRT_BUILD_WIDTH4: the wide BVHs collapse to at most 4 children per node
+ * (same compressed node format) instead of 8. */
+#define GBRT_BUILD_WIDTH4 0x2u
 #define GBRT_FLATTEN_MAX_TRIANGLES (1u << 26)
 int gbrt_blas_build(gbrt_scene* scene, const gbrt_geo_range* ranges, uint32_t n,
                     uint32_t flags);
@@ -430,13 +433,16 @@ int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices)
 
 /* Autotuner (no reference counterpart; the reference leaves traversal to the
  * driver).  Renders a probe frame (probe_ubo's camera, samples and bounces at
- * width x height, into scratch memory) with the binary BVH and with the
- * 8-wide BVH, three rounds each (the first warms up), and keeps the faster
- * layout for this scene's later renders and jobs.  Synchronous. */
+ * width x height, into scratch memory) with the binary BVH, the 8-wide BVH
+ * and the 4-wide BVH (rebuilt for the probe), three rounds each (the first
+ * warms up), and keeps the fastest layout (rebuilding the wide BVH at the
+ * chosen width, which then stands in the scene's build flags) for this
+ * scene's later renders and jobs.  Synchronous. */
 typedef struct gbrt_tune_report {
     double ms_binary;       /* best probe time, binary layout */
     double ms_wide;         /* best probe time, 8-wide layout (0 if the scene has none) */
-    uint32_t chosen_width;  /* 2 or 8 */
+    double ms_wide4;        /* best probe time, 4-wide layout (0 if the scene has none) */
+    uint32_t chosen_width;  /* 2, 4 or 8 */
     uint32_t _pad;
 } gbrt_tune_report;
 int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t width, uint32_t height,

@@ -32,7 +32,7 @@ static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records
 static_assert(sizeof(gbrt_stats) == 104, "stats record");
 static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 64, "job records");
 static_assert(sizeof(gbrt_nrc_config) == 56 && sizeof(gbrt_nrc_render_opts) == 16, "cache records");
-static_assert(sizeof(gbrt_tune_report) == 24, "tune report");
+static_assert(sizeof(gbrt_tune_report) == 32, "tune report");
 
 namespace {
 thread_local std::string g_create_error;
@@ -118,6 +118,8 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
     c->wf.frame_sum = c->wf_frame.as<float4>();
     return e;
 }
+
+int cw_width(const gbrt_scene* s) { return (s->build_flags & GBRT_BUILD_WIDTH4) ? 4 : 8; }
 
 void refresh_view(gbrt_scene* s) {
     DevScene& v = s->view;
@@ -241,7 +243,7 @@ int build_all(gbrt_scene* s) {
         CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
                                    s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)nw,
                                    s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), &s->cw_count, st,
-                                   &s->cw_levels, s->inst.as<DevInstance>()),
+                                   &s->cw_levels, s->inst.as<DevInstance>(), cw_width(s)),
            "build wide world BVH");
         s->nworld = (uint32_t)nw;
     } else {
@@ -284,7 +286,8 @@ int build_all(gbrt_scene* s) {
             CU(c, build_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
                                        s->prims.as<gbrt_priminfo>(), bitems.as<uint4>(), ntri,
                                        s->blas_cw_nodes.as<CwNode>() + cw_node0[g],
-                                       s->blas_cw_tris.as<TriRec>() + cw_tri0[g], &used, st),
+                                       s->blas_cw_tris.as<TriRec>() + cw_tri0[g], &used, st, nullptr, nullptr,
+                                       cw_width(s)),
                "build wide BLAS");
         }
         const uint32_t nt = (uint32_t)tlas_ids.size();
@@ -560,7 +563,7 @@ int gbrt_blas_build(gbrt_scene* s, const gbrt_geo_range* r, uint32_t n, uint32_t
     gbrt_ctx* c = s->ctx;
     if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (n && !r) return fail(c, GBRT_E_INVALID, "ranges is NULL");
-    if (flags & ~GBRT_BUILD_NO_FLATTEN) return fail(c, GBRT_E_INVALID, "unknown build flags");
+    if (flags & ~(GBRT_BUILD_NO_FLATTEN | GBRT_BUILD_WIDTH4)) return fail(c, GBRT_E_INVALID, "unknown build flags");
     s->build_flags = flags;
     for (uint32_t i = 0; i < n; ++i) {
         const gbrt_geo_range& g = r[i];
@@ -778,25 +781,47 @@ int gbrt_scene_autotune(gbrt_scene* s, const gbrt_ubo* ubo, uint32_t width, uint
     out.counters = c->counters.as<DeviceCounters>();
     gbrt_ubo u = *ubo;
     u.total_number_of_samples = u.number_of_samples;
-    double best[2] = {1e30, 1e30};  // [0] binary, [1] 8-wide
-    const bool has_wide = s->view.cw_nodes != nullptr || !s->view.has_world;
-    for (int rep_i = 0; rep_i < 3; ++rep_i)
-        for (int wide = 0; wide < (has_wide ? 2 : 1); ++wide) {
+    // one probe: best of rounds 2 and 3 (the first warms up)
+    auto probe_ms = [&](bool binary, double* best) -> int {
+        *best = 1e30;
+        for (int rep_i = 0; rep_i < 3; ++rep_i) {
             DevScene v = s->view;
-            v.prefer_binary = wide ? 0u : 1u;
+            v.prefer_binary = binary ? 1u : 0u;
             CU(c, cudaEventRecord(c->ev0, st), "event");
             CU(c, launch_wavefront(v, u, out, c->wf, st, nullptr, nullptr, nullptr, &c->side), "probe render");
             CU(c, cudaEventRecord(c->ev1, st), "event");
             CU(c, cudaStreamSynchronize(st), "sync");
             float ms = 0.0f;
             CU(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1), "event time");
-            if (rep_i > 0) best[wide] = std::min(best[wide], (double)ms);  // the first round warms up
+            if (rep_i > 0) *best = std::min(*best, (double)ms);
         }
-    s->view.prefer_binary = (!has_wide || best[0] < best[1]) ? 1u : 0u;
+        return GBRT_OK;
+    };
+    const bool has_wide = s->view.cw_nodes != nullptr || !s->view.has_world;
+    double ms_bin = 0.0, ms_w[2] = {0.0, 0.0};  // [0] 4-wide, [1] 8-wide
+    int rc = probe_ms(true, &ms_bin);
+    if (rc != GBRT_OK) return rc;
+    if (has_wide) {
+        const int w0 = cw_width(s) == 4 ? 0 : 1;
+        if ((rc = probe_ms(false, &ms_w[w0])) != GBRT_OK) return rc;
+        // the other width: rebuild, probe
+        s->build_flags ^= GBRT_BUILD_WIDTH4;
+        if ((rc = build_all(s)) != GBRT_OK) return rc;
+        if ((rc = probe_ms(false, &ms_w[1 - w0])) != GBRT_OK) return rc;
+        const int wbest = ms_w[0] < ms_w[1] ? 0 : 1;
+        if (wbest != 1 - w0) {  // the first width was faster: rebuild it
+            s->build_flags ^= GBRT_BUILD_WIDTH4;
+            if ((rc = build_all(s)) != GBRT_OK) return rc;
+        }
+        s->view.prefer_binary = ms_bin < ms_w[wbest] ? 1u : 0u;
+    } else {
+        s->view.prefer_binary = 1u;
+    }
     if (rep) {
-        rep->ms_binary = best[0];
-        rep->ms_wide = has_wide ? best[1] : 0.0;
-        rep->chosen_width = s->view.prefer_binary ? 2u : 8u;
+        rep->ms_binary = ms_bin;
+        rep->ms_wide = ms_w[1];
+        rep->ms_wide4 = ms_w[0];
+        rep->chosen_width = s->view.prefer_binary ? 2u : (uint32_t)cw_width(s);
         rep->_pad = 0;
     }
     return GBRT_OK;

@@ -88,7 +88,7 @@ struct gbrt_scene {
     std::vector<uint32_t> cw_levels;  // first node of each level of the 8-wide world BVH (for refit)
     gbrt_host::DevBuf cw_boxes;        // refit scratch: float boxes of the 8-wide nodes
     uint32_t nworld = 0;               // triangles in the world BVH
-    uint32_t build_flags = 0;          // gbrt_blas_build flags (GBRT_BUILD_NO_FLATTEN)
+    uint32_t build_flags = 0;          // gbrt_blas_build flags (GBRT_BUILD_NO_FLATTEN, GBRT_BUILD_WIDTH4)
     uint32_t cw_count = 0;
     bool built = false;
     std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene

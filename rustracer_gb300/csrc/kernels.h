@@ -213,11 +213,12 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_v
 
 // Compressed 8-wide BVH over n triangle items: nodes (capacity n, root at 0)
 // and their triangles (n slots, node-leaf order); *nodes_used (host) gets
-// the node count.
+// the node count.  width 4 collapses to at most 4 children per node (same
+// node format, so the same traversal).
 cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  const uint4* items, uint32_t n, CwNode* nodes, TriRec* tris, uint32_t* nodes_used,
                                  cudaStream_t st, std::vector<uint32_t>* level_starts = nullptr,
-                                 const DevInstance* inst = nullptr);
+                                 const DevInstance* inst = nullptr, int width = 8);
 // Refit of an 8-wide BVH built by build_triangle_cwbvh over the same
 // triangles: triangle records re-read from the vertices, then every node's
 // grid and child boxes recomputed level by level (level_starts: first node

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgbrt.so"
 
 OK, E_INVALID, E_CUDA, E_OOM, E_DEVICE_LIMIT, E_NOT_BUILT, E_NO_DEVICE, E_BUSY = 0, -1, -2, -3, -4, -5, -6, -7
 BUILD_NO_FLATTEN = 0x1
+BUILD_WIDTH4 = 0x2
 MODE_AUTO, MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1, 2
 
 # name -> (restype, argtypes); every symbol include/gbrt.h declares
@@ -381,12 +382,13 @@ class Scene:
         self.ctx.check(self.ctx.L.gbrt_skybox_set(self.h, size, _p(faces)))
 
     def autotune(self, ubo, width, height):
-        """gbrt_scene_autotune: picks the faster BVH layout; returns
-        dict(ms_binary, ms_wide, chosen_width)."""
-        rep = np.zeros(3, np.float64)
+        """gbrt_scene_autotune: picks the fastest BVH layout (binary, 4- or
+        8-wide); returns dict(ms_binary, ms_wide, ms_wide4, chosen_width)."""
+        rep = np.zeros(4, np.float64)
         ubo = np.asarray(ubo, T.UBO).reshape(())
         self.ctx.check(self.ctx.L.gbrt_scene_autotune(self.h, _p(ubo), width, height, _p(rep)))
-        return dict(ms_binary=float(rep[0]), ms_wide=float(rep[1]), chosen_width=int(rep[2:].view(np.uint32)[0]))
+        return dict(ms_binary=float(rep[0]), ms_wide=float(rep[1]), ms_wide4=float(rep[2]),
+                    chosen_width=int(rep[3:].view(np.uint32)[0]))
 
     def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False):
         """One frame (record_raytracing_commands + the shaders).  Returns a dict

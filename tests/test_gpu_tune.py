@@ -1,5 +1,5 @@
-"""Autotuner: both BVH layouts give the same image bit for bit, so the
-layout gbrt_scene_autotune keeps changes speed only."""
+"""Autotuner: the binary, 4-wide and 8-wide BVH layouts give the same image
+bit for bit, so the layout gbrt_scene_autotune keeps changes speed only."""
 import numpy as np
 import pytest
 
@@ -16,9 +16,26 @@ def test_autotune_keeps_results(gpu_ctx):
     a0 = gbrt.Accum(gpu_ctx, 160, 120)
     before = sc.render(ubo, a0, mode=gbrt.MODE_WAVEFRONT)["image"]
     rep = sc.autotune(sd.ubo(256, 256, samples=2, bounces=6, exposure=1.0), 256, 256)
-    assert rep["chosen_width"] in (2, 8)
-    assert rep["ms_binary"] > 0 and rep["ms_wide"] > 0
+    assert rep["chosen_width"] in (2, 4, 8)
+    assert rep["ms_binary"] > 0 and rep["ms_wide"] > 0 and rep["ms_wide4"] > 0
     a1 = gbrt.Accum(gpu_ctx, 160, 120)
     after = sc.render(ubo, a1, mode=gbrt.MODE_WAVEFRONT)["image"]
     assert np.array_equal(before, after)
     assert np.array_equal(a0.download(), a1.download())
+
+
+@pytest.mark.parametrize("flatten", [True, False], ids=["flattened", "tlas"])
+def test_width4_equals_width8(gpu_ctx, flatten):
+    """The 4-wide build (world BVH, or BLASes under a TLAS) renders the 8-wide build's image bit for bit."""
+    from rustracer_gb300 import gbrt, zoo
+    sd = zoo.material_zoo(subdiv=3)
+    base = 0 if flatten else gbrt.BUILD_NO_FLATTEN
+    out = []
+    for flags in (base, base | gbrt.BUILD_WIDTH4):
+        sc = gbrt.Scene(gpu_ctx, sd, build_flags=flags)
+        acc = gbrt.Accum(gpu_ctx, 160, 120)
+        img = sc.render(sd.ubo(160, 120, samples=3, bounces=6, exposure=1.0, has_sky=True), acc,
+                        mode=gbrt.MODE_WAVEFRONT)["image"]
+        out.append((img, acc.download()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
