@@ -362,6 +362,11 @@ def run_batched(args):
     accs = [gbrt.Accum(ctx, w, h) for _, w, h, _ in specs]
     ubos = [sd.ubo(w, h, samples=spp, bounces=depth, exposure=1.0) for sd, w, h, spp in specs]
     pinned = [np.zeros((h, w, 4), np.uint8) for _, w, h, _ in specs]
+    # autotuner (setup, untimed): per scene, a 256x144 1-spp probe of each BVH layout
+    t_tune = time.perf_counter()
+    tuned = [sc.autotune(sd.ubo(256, 144, samples=1, bounces=depth, exposure=1.0), 256, 144)
+             for sc, (sd, _, _, _) in zip(scs, specs)]
+    t_tune = time.perf_counter() - t_tune
 
     def batch():
         jobs = [ctx.submit(sc, u, a) for sc, u, a in zip(scs, ubos, accs)]
@@ -418,6 +423,9 @@ def run_batched(args):
                          "bytes_per_ray_by_scene": [round(b, 1) for b in brays]},
             "sequential": {"value": seq_rays / seq_wall / 1e6, "unit": "Mrays/s",
                            "how": "the same 32 frames one after another through gbrt_render_ex"},
+            "autotune": {"seconds": round(t_tune, 3),
+                         "chosen_width": {str(w): sum(t["chosen_width"] == w for t in tuned) for w in (2, 4, 8)},
+                         "probe": "256x144, 1 spp, binary / 4-wide / 8-wide, best of 2 after a warm-up"},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * 324,
                     "d2h_bytes_per_step": int(sum(w * h * 4 for _, w, h, _ in specs))},
             "clocks": clocks}
