@@ -367,6 +367,7 @@ def run_batched(args):
     tuned = [sc.autotune(sd.ubo(256, 144, samples=1, bounces=depth, exposure=1.0), 256, 144)
              for sc, (sd, _, _, _) in zip(scs, specs)]
     t_tune = time.perf_counter() - t_tune
+    ctx.jobs_configure(policy=gbrt.POLICY_SRPT | gbrt.JOB_LARGE_WAVES)  # throughput: waves up to 2^26 paths
 
     def batch():
         jobs = [ctx.submit(sc, u, a) for sc, u, a in zip(scs, ubos, accs)]
@@ -417,7 +418,8 @@ def run_batched(args):
                        "instances": int(sum(len(sd.instances) for sd, _, _, _ in specs)),
                        "paths_per_step": int(px), "depth": depth,
                        "resolutions": "{256^2, 512^2, 1280x720, 1920x1080}", "spp": "{1, 4, 16, 64}",
-                       "l2": "inputs (1.2 GB of vertices) larger than L2", "timing": "host wall clock, submit to last image on host"},
+                       "l2": "inputs (1.2 GB of vertices) larger than L2", "timing": "host wall clock, submit to last image on host",
+                       "waves": "up to 2^26 paths (GBRT_JOB_LARGE_WAVES)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind, "kernel": "whole batch (algorithmic bytes)",
                          "bytes_per_ray_by_scene": [round(b, 1) for b in brays]},

@@ -485,6 +485,10 @@ int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t w
 #define GBRT_JOB_DONE     2u
 #define GBRT_JOB_POLICY_SRPT 0u
 #define GBRT_JOB_POLICY_FIFO 1u
+/* OR into the policy: on a deep queue waves grow to 2^26 paths instead of
+ * 2^24 (throughput over latency).  Set it before the context's first submit:
+ * the wave buffers (216 B per path) are sized then. */
+#define GBRT_JOB_LARGE_WAVES 0x100u
 
 typedef struct gbrt_job_desc {
     gbrt_scene* scene;

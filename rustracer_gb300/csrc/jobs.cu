@@ -38,15 +38,14 @@ double now_ms() {
 }
 
 // paths per batched wave: 2^22 while little work is queued, so that a wave,
-// and the wait of a job that joins the batch, stays short; growing to 2^26
-// (a quarter of the queued paths) when a deep queue makes throughput matter
-// (32 frames of 1.0G paths in all: 1257 Mrays/s with a 2^24 limit, 1312 with 2^26)
+// and the wait of a job that joins the batch, stays short; growing to a
+// quarter of the queued paths on a deep queue, at most 2^24 (latency: 200
+// Poisson jobs over 8 scenes gave p50 2.5 s with 2^24, 3.3 s with 2^26) or
+// 2^26 with GBRT_JOB_LARGE_WAVES (throughput: 32 frames of 1.0G paths gave
+// 1257 Mrays/s with 2^24, 1312 with 2^26)
 constexpr uint32_t kWaveCap = kMaxWavePaths < (1u << 22) ? kMaxWavePaths : (1u << 22);
-#ifndef GBRT_WAVE_CAP_DEEP_LOG2
-#define GBRT_WAVE_CAP_DEEP_LOG2 26
-#endif
-constexpr uint32_t kWaveCapDeep =
-    kMaxWavePaths < (1u << GBRT_WAVE_CAP_DEEP_LOG2) ? kMaxWavePaths : (1u << GBRT_WAVE_CAP_DEEP_LOG2);
+constexpr uint32_t kWaveCapDeep = kMaxWavePaths < (1u << 24) ? kMaxWavePaths : (1u << 24);
+constexpr uint32_t kWaveCapLarge = kMaxWavePaths < (1u << 26) ? kMaxWavePaths : (1u << 26);
 constexpr uint32_t kChunkDiv = 8;             // pixel chunk = wave / 8 (finer packing)
 constexpr int kMaxInFlight = 2;
 
@@ -118,6 +117,7 @@ struct JobQueue {
     uint32_t outstanding = 0;  // submitted and not finished
     uint64_t budget = 0, used = 0;
     uint32_t policy = GBRT_JOB_POLICY_SRPT;
+    uint32_t deep_cap = kWaveCapDeep;  // kWaveCapLarge with GBRT_JOB_LARGE_WAVES
     bool stop = false;
     std::thread worker;
     cudaStream_t dl = nullptr;  // downloads of finished jobs (non-blocking stream)
@@ -221,7 +221,7 @@ int JobQueue::pack_and_launch() {
     std::vector<Job*> finishing;
     uint64_t queued = 0;
     for (const Job* j : order) queued += j->paths_left;
-    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(queued / 4, kWaveCap), kWaveCapDeep);
+    const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(queued / 4, kWaveCap), deep_cap);
     uint32_t room = std::min(cap, ctx->wf.cap);
     for (Job* j : order) {
         if (w->njobs == (uint32_t)kMaxWaveJobs || w->nsegs == (uint32_t)kMaxWaveSegs || room == 0) break;
@@ -482,12 +482,14 @@ extern "C" {
 
 int gbrt_jobs_configure(gbrt_ctx* c, uint64_t budget, uint32_t policy) {
     if (!c) return GBRT_E_INVALID;
-    if (policy > GBRT_JOB_POLICY_FIFO) return fail(c, GBRT_E_INVALID, "unknown job policy");
+    if ((policy & ~GBRT_JOB_LARGE_WAVES) > GBRT_JOB_POLICY_FIFO) return fail(c, GBRT_E_INVALID, "unknown job policy");
     std::lock_guard<std::mutex> lk(c->mu);
     if (c->jobs) {
         std::lock_guard<std::mutex> lq(c->jobs->mu);
         if (budget) c->jobs->budget = budget;
-        c->jobs->policy = policy;
+        c->jobs->policy = policy & ~GBRT_JOB_LARGE_WAVES;
+        // the wave buffers were sized at the first submit: larger waves only up to them
+        c->jobs->deep_cap = std::min((policy & GBRT_JOB_LARGE_WAVES) ? kWaveCapLarge : kWaveCapDeep, c->wf.cap);
         return GBRT_OK;
     }
     c->jobs_budget = budget;
@@ -535,13 +537,14 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
             DeviceGuard g(c->device);
             auto q = std::make_unique<JobQueue>();
             q->ctx = c;
-            q->policy = c->jobs_policy;
+            q->policy = c->jobs_policy & ~GBRT_JOB_LARGE_WAVES;
+            q->deep_cap = (c->jobs_policy & GBRT_JOB_LARGE_WAVES) ? kWaveCapLarge : kWaveCapDeep;
             size_t fr = 0, tot = 0;
             cudaError_t e = cudaMemGetInfo(&fr, &tot);
             const uint64_t gib = 1ull << 30;
             q->budget = c->jobs_budget ? c->jobs_budget : (fr > gib ? fr - gib : fr / 2);
             if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&q->dl, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = wavefront_reserve(c, kWaveCapDeep, 0) == cudaSuccess ? cudaSuccess : cudaErrorMemoryAllocation;
+            if (e == cudaSuccess) e = wavefront_reserve(c, q->deep_cap, 0) == cudaSuccess ? cudaSuccess : cudaErrorMemoryAllocation;
             if (e != cudaSuccess) {
                 if (q->dl) cudaStreamDestroy(q->dl);
                 return cuda_fail(c, e, "job scheduler setup");

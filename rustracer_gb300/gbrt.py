@@ -74,6 +74,7 @@ SIGNATURES = {
 }
 JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
 POLICY_SRPT, POLICY_FIFO = 0, 1
+JOB_LARGE_WAVES = 0x100  # OR into the policy before the first submit: waves up to 2^26 paths
 NOALLOC_MAX_TRIANGLES = 65536
 
 

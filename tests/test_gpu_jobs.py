@@ -169,3 +169,26 @@ def test_cache_calls_busy_while_jobs_outstanding(gpu_ctx):
     assert e.value.code == gbrt.E_BUSY
     assert job.wait()["status"] == 0
     assert c.query(np.zeros((4, 3), np.float32)).shape == (4, 3)
+
+
+def test_large_waves_equal_solo_render():
+    """GBRT_JOB_LARGE_WAVES (waves up to 2^26 paths on a deep queue): a
+    frame of 83M paths as a job equals the solo render, beside a small job."""
+    from rustracer_gb300 import build, gbrt
+    build.build()
+    ctx = gbrt.Context(0)
+    try:
+        ctx.jobs_configure(policy=gbrt.POLICY_SRPT | gbrt.JOB_LARGE_WAVES)
+        sd = scenes.icosphere_scene(subdiv=3)
+        sc = gbrt.Scene(ctx, sd)
+        big = sd.ubo(1920, 1080, samples=40, bounces=4, exposure=1.0)
+        small = sd.ubo(64, 64, samples=2, bounces=4, exposure=1.0)
+        ref = [_solo(ctx, sc, u, w, h) for u, w, h in ((big, 1920, 1080), (small, 64, 64))]
+        accs = [gbrt.Accum(ctx, 1920, 1080), gbrt.Accum(ctx, 64, 64)]
+        js = [ctx.submit(sc, big, accs[0]), ctx.submit(sc, small, accs[1])]
+        for j, a, (img, acc_ref) in zip(js, accs, ref):
+            assert j.wait()["status"] == 0
+            assert np.array_equal(j.image.reshape(img.shape), img)
+            assert np.array_equal(a.download(), acc_ref)
+    finally:
+        ctx.close()
