@@ -210,6 +210,12 @@ def run_gpu(args):
     ctx = gbrt.Context(local)
     scene = gbrt.Scene(ctx, sd)
     acc = gbrt.Accum(ctx, W, H)
+    # traversal layout and ray-sort key: the autotuner's choice (untimed setup) or fixed
+    if args.tune == "auto":
+        tuning = scene.autotune(sd.ubo(W, H, samples=SPP, bounces=DEPTH, exposure=1.0), W, H)  # one step's frame
+    else:
+        tuning = {"chosen_width": int(args.tune[1]), "sort_rays": int(args.tune.endswith("s"))}
+        scene.set_tuning(tuning["chosen_width"], bool(tuning["sort_rays"]))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     pinned = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
     state = {"step": 0}
@@ -308,7 +314,8 @@ def run_gpu(args):
     traffic = traffic_from_profile(kernel_name, rays_per_launch)
     line = common_line(args, world, value, dev_ms / args.steps,
                        {"kernel": args.mode, "wall_ms_per_step": wall / args.steps * 1e3,
-                        "launches_per_step": launches})
+                        "launches_per_step": launches,
+                        "tuning": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tuning.items()}})
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": traffic, "peak_source": peak_kind,
                         "bytes_per_ray": bray, "n_node": n_node, "n_tri": n_tri,
@@ -362,9 +369,9 @@ def run_batched(args):
     accs = [gbrt.Accum(ctx, w, h) for _, w, h, _ in specs]
     ubos = [sd.ubo(w, h, samples=spp, bounces=depth, exposure=1.0) for sd, w, h, spp in specs]
     pinned = [np.zeros((h, w, 4), np.uint8) for _, w, h, _ in specs]
-    # autotuner (setup, untimed): per scene, a 256x144 1-spp probe of each BVH layout
+    # autotuner (setup, untimed): per scene, a 640x360 2-spp probe of each BVH layout and the ray-sort key
     t_tune = time.perf_counter()
-    tuned = [sc.autotune(sd.ubo(256, 144, samples=1, bounces=depth, exposure=1.0), 256, 144)
+    tuned = [sc.autotune(sd.ubo(640, 360, samples=2, bounces=depth, exposure=1.0), 640, 360)
              for sc, (sd, _, _, _) in zip(scs, specs)]
     t_tune = time.perf_counter() - t_tune
     ctx.jobs_configure(policy=gbrt.POLICY_SRPT | gbrt.JOB_LARGE_WAVES)  # throughput: waves up to 2^26 paths
@@ -427,7 +434,8 @@ def run_batched(args):
                            "how": "the same 32 frames one after another through gbrt_render_ex"},
             "autotune": {"seconds": round(t_tune, 3),
                          "chosen_width": {str(w): sum(t["chosen_width"] == w for t in tuned) for w in (2, 4, 8)},
-                         "probe": "256x144, 1 spp, binary / 4-wide / 8-wide, best of 2 after a warm-up"},
+                         "sort_rays": sum(t["sort_rays"] for t in tuned),
+                         "probe": "640x360, 2 spp, binary / 4-wide / 8-wide, then the ray-sort key; best of 2 after a warm-up"},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * 324,
                     "d2h_bytes_per_step": int(sum(w * h * 4 for _, w, h, _ in specs))},
             "clocks": clocks}
@@ -653,6 +661,8 @@ def main():
     ap.add_argument("--mode", default="auto", choices=list(MODES), help="kernel form (auto = wavefront)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
+    ap.add_argument("--tune", default="auto", choices=["auto", "w2", "w4", "w8", "w2s", "w4s", "w8s"],
+                    help="icosphere: autotuner (untimed setup) or a fixed BVH width w2/w4/w8, s = ray-sort key on")
     ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched", "serving", "nrc"],
                     help="icosphere: the headline frame; batched: 32 scenes as one batch of jobs; "

@@ -434,19 +434,28 @@ int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices)
 /* Autotuner (no reference counterpart; the reference leaves traversal to the
  * driver).  Renders a probe frame (probe_ubo's camera, samples and bounces at
  * width x height, into scratch memory) with the binary BVH, the 8-wide BVH
- * and the 4-wide BVH (rebuilt for the probe), three rounds each (the first
- * warms up), and keeps the fastest layout (rebuilding the wide BVH at the
- * chosen width, which then stands in the scene's build flags) for this
- * scene's later renders and jobs.  Synchronous. */
+ * and the 4-wide BVH (rebuilt for the probe), each with the ray-sort key off
+ * and on (on: shading writes each block's extension rays grouped by
+ * direction octant, so traversal warps see more coherent rays), three rounds
+ * each (the first warms up), and keeps the fastest pair (rebuilding the wide
+ * BVH at the chosen width, which then stands in the scene's build flags) for
+ * this scene's later renders and jobs.  No choice changes any result bit.
+ * The probe should resemble the frames to come: differences between layouts
+ * are a few percent.  Synchronous. */
 typedef struct gbrt_tune_report {
     double ms_binary;       /* best probe time, binary layout */
     double ms_wide;         /* best probe time, 8-wide layout (0 if the scene has none) */
     double ms_wide4;        /* best probe time, 4-wide layout (0 if the scene has none) */
+    double ms_sorted;       /* best probe time, chosen layout with the ray-sort key (the other times: key off) */
     uint32_t chosen_width;  /* 2, 4 or 8 */
-    uint32_t _pad;
+    uint32_t sort_rays;     /* 1: ray-sort key kept */
 } gbrt_tune_report;
 int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t width, uint32_t height,
                         gbrt_tune_report* report);
+/* Sets the autotuner's two choices directly: BVH width 2 (binary), 4 or 8
+ * (rebuilding the wide BVHs when the width changes) and the ray-sort key
+ * (sort_rays != 0).  Synchronous. */
+int gbrt_scene_set_tuning(gbrt_scene* scene, uint32_t width, uint32_t sort_rays);
 
 /* ------------------------------------------------------------------------ */
 /* Jobs: asynchronous frames with continuous batching                       */

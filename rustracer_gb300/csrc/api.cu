@@ -32,7 +32,7 @@ static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records
 static_assert(sizeof(gbrt_stats) == 104, "stats record");
 static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 64, "job records");
 static_assert(sizeof(gbrt_nrc_config) == 56 && sizeof(gbrt_nrc_render_opts) == 16, "cache records");
-static_assert(sizeof(gbrt_tune_report) == 32, "tune report");
+static_assert(sizeof(gbrt_tune_report) == 40, "tune report");
 
 namespace {
 thread_local std::string g_create_error;
@@ -798,32 +798,66 @@ int gbrt_scene_autotune(gbrt_scene* s, const gbrt_ubo* ubo, uint32_t width, uint
         return GBRT_OK;
     };
     const bool has_wide = s->view.cw_nodes != nullptr || !s->view.has_world;
-    double ms_bin = 0.0, ms_w[2] = {0.0, 0.0};  // [0] 4-wide, [1] 8-wide
-    int rc = probe_ms(true, &ms_bin);
+    // ms[layout][sort]: layout 0 binary, 1 4-wide, 2 8-wide
+    double ms[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+    auto probe_both = [&](int layout) -> int {
+        for (int so = 0; so < 2; ++so) {
+            s->view.sort_rays = (uint32_t)so;
+            const int r = probe_ms(layout == 0, &ms[layout][so]);
+            if (r != GBRT_OK) return r;
+        }
+        return GBRT_OK;
+    };
+    int rc = probe_both(0);
     if (rc != GBRT_OK) return rc;
+    int best_l = 0, best_s = ms[0][1] < ms[0][0] ? 1 : 0;
     if (has_wide) {
-        const int w0 = cw_width(s) == 4 ? 0 : 1;
-        if ((rc = probe_ms(false, &ms_w[w0])) != GBRT_OK) return rc;
+        const int l0 = cw_width(s) == 4 ? 1 : 2;
+        if ((rc = probe_both(l0)) != GBRT_OK) return rc;
         // the other width: rebuild, probe
         s->build_flags ^= GBRT_BUILD_WIDTH4;
         if ((rc = build_all(s)) != GBRT_OK) return rc;
-        if ((rc = probe_ms(false, &ms_w[1 - w0])) != GBRT_OK) return rc;
-        const int wbest = ms_w[0] < ms_w[1] ? 0 : 1;
-        if (wbest != 1 - w0) {  // the first width was faster: rebuild it
+        if ((rc = probe_both(3 - l0)) != GBRT_OK) return rc;
+        for (int l = 1; l < 3; ++l)
+            for (int so = 0; so < 2; ++so)
+                if (ms[l][so] < ms[best_l][best_s]) {
+                    best_l = l;
+                    best_s = so;
+                }
+        // keep the wide BVH at the better width (the binary one is the same either way)
+        const int keep = best_l ? best_l : (std::min(ms[1][0], ms[1][1]) < std::min(ms[2][0], ms[2][1]) ? 1 : 2);
+        if (keep == l0) {
             s->build_flags ^= GBRT_BUILD_WIDTH4;
             if ((rc = build_all(s)) != GBRT_OK) return rc;
         }
-        s->view.prefer_binary = ms_bin < ms_w[wbest] ? 1u : 0u;
-    } else {
-        s->view.prefer_binary = 1u;
     }
+    s->view.prefer_binary = best_l == 0 ? 1u : 0u;
+    s->view.sort_rays = (uint32_t)best_s;
     if (rep) {
-        rep->ms_binary = ms_bin;
-        rep->ms_wide = ms_w[1];
-        rep->ms_wide4 = ms_w[0];
-        rep->chosen_width = s->view.prefer_binary ? 2u : (uint32_t)cw_width(s);
-        rep->_pad = 0;
+        rep->ms_binary = ms[0][0];
+        rep->ms_wide = ms[2][0];
+        rep->ms_wide4 = ms[1][0];
+        rep->ms_sorted = ms[best_l][1];
+        rep->chosen_width = best_l == 0 ? 2u : (uint32_t)cw_width(s);
+        rep->sort_rays = s->view.sort_rays;
     }
+    return GBRT_OK;
+}
+
+int gbrt_scene_set_tuning(gbrt_scene* s, uint32_t width, uint32_t sort_rays) {
+    if (!s) return GBRT_E_INVALID;
+    gbrt_ctx* c = s->ctx;
+    if (width != 2 && width != 4 && width != 8) return fail(c, GBRT_E_INVALID, "width must be 2, 4 or 8");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the BLAS and TLAS before tuning");
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
+    DeviceGuard g(c->device);
+    if (width != 2 && (uint32_t)cw_width(s) != width) {
+        s->build_flags ^= GBRT_BUILD_WIDTH4;
+        const int rc = build_all(s);
+        if (rc != GBRT_OK) return rc;
+    }
+    s->view.prefer_binary = width == 2 ? 1u : 0u;
+    s->view.sort_rays = sort_rays ? 1u : 0u;
     return GBRT_OK;
 }
 

@@ -106,6 +106,7 @@ struct DevScene {
     uint32_t sky_size;
     uint32_t all_opaque; // every geometry is OPAQUE: the any-hit test never runs
     uint32_t prefer_binary;  // autotuner's choice: traverse the binary layout even where 8-wide nodes exist
+    uint32_t sort_rays;      // autotuner's choice: shade writes each block's extension rays grouped by octant
 };
 
 }  // namespace gbrt

@@ -45,6 +45,36 @@ GB_D uint32_t warp_append(uint32_t* counter, bool want) {
     return base + __popc(mask & ((1u << lane_id()) - 1u));
 }
 
+// Block-wide queue append grouped by a 3-bit key (the ray's direction
+// octant): the block's wanted entries get one contiguous range of the queue,
+// key 0 first, so a warp that later takes consecutive entries sees rays of
+// few octants.  Order within a key is unspecified (every consumer indexes
+// path state by the path id the entry carries).  Every thread of the block
+// calls it; s: 17 words of shared memory.
+GB_D uint32_t block_append_by_key(uint32_t* counter, bool want, uint32_t key, uint32_t* s) {
+    if (threadIdx.x < 8) s[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, want ? key : 8u);
+    uint32_t base = 0;
+    const uint32_t leader = __ffs(peers) - 1u;
+    if (want && lane_id() == leader) base = atomicAdd(&s[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    const uint32_t rank = base + __popc(peers & ((1u << lane_id()) - 1u));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int k = 0; k < 8; ++k) {
+            s[8 + k] = tot;
+            tot += s[k];
+        }
+        s[16] = tot ? atomicAdd(counter, tot) : 0u;
+    }
+    __syncthreads();
+    return want ? s[16] + s[8 + key] + rank : 0u;
+}
+
+GB_D uint32_t octant_of(float3 d) { return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u); }
+
 template <class T>
 GB_D T warp_sum(T v) {
 #pragma unroll
@@ -193,8 +223,11 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
     PathStats ps{0, 0, 0, 0, 0};
     const uint32_t blk0 = w.blk0(1, jb), nblk = w.nblk(1, jb);
     const uint32_t stride = nblk * blockDim.x;
-    for (uint32_t base = (blockIdx.x - blk0) * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
-        const uint32_t q = base + lane_id();
+    const bool sort_rays = s.sort_rays != 0u;
+    __shared__ uint32_t s_key[17];
+    // block-uniform trip count (block_append_by_key synchronises the block)
+    for (uint32_t cbase = (blockIdx.x - blk0) * blockDim.x; cbase < n; cbase += stride) {
+        const uint32_t q = cbase + threadIdx.x;
         const bool active = q < n;
         bool cont = false, shadow = false;
         float3 nxt_o = f3(0.0f), nxt_d = f3(0.0f), so = f3(0.0f), sd = f3(0.0f), sc = f3(0.0f), se = f3(0.0f);
@@ -284,7 +317,8 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             nxt_d = Rp.scatterDir;
             }
         }
-        const uint32_t slot = warp_append(&cnt[kQueue + b + 1], cont);
+        const uint32_t slot = sort_rays ? block_append_by_key(&cnt[kQueue + b + 1], cont, octant_of(nxt_d), s_key)
+                                        : warp_append(&cnt[kQueue + b + 1], cont);
         if (cont) {
             no[slot] = f4(nxt_o, 0.0f);
             nd[slot] = f4(nxt_d, __uint_as_float(word));

@@ -71,6 +71,7 @@ SIGNATURES = {
     "gbrt_nrc_train": (i32, [P, P, P, u32, i32, P, P, P]),
     "gbrt_render_nrc": (i32, [P, P, P, P, P, P, P, P]),
     "gbrt_scene_autotune": (i32, [P, P, u32, u32, P]),
+    "gbrt_scene_set_tuning": (i32, [P, u32, u32]),
 }
 JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
 POLICY_SRPT, POLICY_FIFO = 0, 1
@@ -384,12 +385,18 @@ class Scene:
 
     def autotune(self, ubo, width, height):
         """gbrt_scene_autotune: picks the fastest BVH layout (binary, 4- or
-        8-wide); returns dict(ms_binary, ms_wide, ms_wide4, chosen_width)."""
-        rep = np.zeros(4, np.float64)
+        8-wide) and whether to group extension rays by octant; returns
+        dict(ms_binary, ms_wide, ms_wide4, ms_sorted, chosen_width, sort_rays)."""
+        rep = np.zeros(5, np.float64)
         ubo = np.asarray(ubo, T.UBO).reshape(())
         self.ctx.check(self.ctx.L.gbrt_scene_autotune(self.h, _p(ubo), width, height, _p(rep)))
+        u = rep[4:].view(np.uint32)
         return dict(ms_binary=float(rep[0]), ms_wide=float(rep[1]), ms_wide4=float(rep[2]),
-                    chosen_width=int(rep[3:].view(np.uint32)[0]))
+                    ms_sorted=float(rep[3]), chosen_width=int(u[0]), sort_rays=int(u[1]))
+
+    def set_tuning(self, width=8, sort_rays=False):
+        """gbrt_scene_set_tuning: BVH width 2/4/8 and the ray-sort key, set directly."""
+        self.ctx.check(self.ctx.L.gbrt_scene_set_tuning(self.h, width, int(bool(sort_rays))))
 
     def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False):
         """One frame (record_raytracing_commands + the shaders).  Returns a dict

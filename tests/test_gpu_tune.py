@@ -1,5 +1,6 @@
-"""Autotuner: the binary, 4-wide and 8-wide BVH layouts give the same image
-bit for bit, so the layout gbrt_scene_autotune keeps changes speed only."""
+"""Autotuner: the binary, 4-wide and 8-wide BVH layouts, and extension rays
+grouped by octant or not, give the same image bit for bit, so what
+gbrt_scene_autotune keeps changes speed only."""
 import numpy as np
 import pytest
 
@@ -17,7 +18,8 @@ def test_autotune_keeps_results(gpu_ctx):
     before = sc.render(ubo, a0, mode=gbrt.MODE_WAVEFRONT)["image"]
     rep = sc.autotune(sd.ubo(256, 256, samples=2, bounces=6, exposure=1.0), 256, 256)
     assert rep["chosen_width"] in (2, 4, 8)
-    assert rep["ms_binary"] > 0 and rep["ms_wide"] > 0 and rep["ms_wide4"] > 0
+    assert rep["ms_binary"] > 0 and rep["ms_wide"] > 0 and rep["ms_wide4"] > 0 and rep["ms_sorted"] > 0
+    assert rep["sort_rays"] in (0, 1)
     a1 = gbrt.Accum(gpu_ctx, 160, 120)
     after = sc.render(ubo, a1, mode=gbrt.MODE_WAVEFRONT)["image"]
     assert np.array_equal(before, after)
@@ -39,3 +41,25 @@ def test_width4_equals_width8(gpu_ctx, flatten):
         out.append((img, acc.download()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("width", [2, 8])
+def test_sorted_rays_equal_unsorted(gpu_ctx, width):
+    """Extension rays grouped by octant (single-frame waves and batched job
+    waves) render the ungrouped image bit for bit."""
+    from rustracer_gb300 import gbrt, zoo
+    sd = zoo.material_zoo(subdiv=3)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    ubo = sd.ubo(200, 150, samples=3, bounces=8, exposure=1.0, has_sky=True)
+    out = []
+    for sort in (False, True):
+        sc.set_tuning(width, sort)
+        acc = gbrt.Accum(gpu_ctx, 200, 150)
+        out.append((sc.render(ubo, acc, mode=gbrt.MODE_WAVEFRONT)["image"], acc.download()))
+    acc = gbrt.Accum(gpu_ctx, 200, 150)
+    job = gpu_ctx.submit(sc, ubo, acc)  # sorting still on
+    assert job.wait()["status"] == 0
+    out.append((job.image.reshape(out[0][0].shape), acc.download()))
+    for img, a in out[1:]:
+        assert np.array_equal(out[0][0], img)
+        assert np.array_equal(out[0][1], a)
