@@ -373,7 +373,7 @@ int refit_world(gbrt_scene* s) {
     BvhResult r;
     CU(c, build_triangle_bvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
                              s->items.as<uint4>(), s->nworld, s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r,
-                             st, s->inst.as<DevInstance>()),
+                             st, s->inst.as<DevInstance>(), kBvhFast),
        "rebuild world BVH");
     CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4)), "cudaMalloc(refit boxes)");
     CU(c, refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),

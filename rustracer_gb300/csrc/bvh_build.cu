@@ -1,14 +1,19 @@
 // bvh_build.cu — GPU BVH construction.
 //
-// Linear BVH (Karras 2012, "Maximizing Parallelism in the Construction of
-// BVHs, Octrees, and k-d Trees"): 30-bit Morton codes of the item centroids,
-// CUB radix sort, one thread per inner node to find its key range and split,
-// then one bottom-up pass (atomic arrival counters) that computes the boxes
+// 30-bit Morton codes of the item centroids and a CUB radix sort, then a
+// binary tree: by default parallel locally-ordered clustering
+// (ploc_build.inc), or, for fast rebuilds, the linear BVH of Karras 2012
+// ("Maximizing Parallelism in the Construction of BVHs, Octrees, and k-d
+// Trees": one thread per inner node finds its key range and split); then one
+// bottom-up pass (atomic arrival counters) that computes the boxes
 // and the SAH cost of every subtree and collapses subtrees of at most
 // kMaxLeaf items into leaves when that lowers the SAH cost.  The result is
 // written in the traversal layout (BNode2 with both child boxes; leaves as
 // codes over a contiguous range of TriRec slots in Morton order).
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <cstring>
+#include <utility>
 #include <float.h>
 #include "kernels.h"
 
@@ -341,18 +346,29 @@ void scratch_free(Scratch& s, cudaStream_t st) {
         if (p) cudaFreeAsync(p, st);
 }
 
-// Morton codes, sort, radix tree and the bottom-up pass (boxes, SAH costs,
-// leaf collapse with at most max_leaf items).  Item boxes in s.lo/hi and
-// centroid bounds in s.cbounds must be ready.
-cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t st) {
+}  // namespace
+
+#include "ploc_build.inc"
+
+namespace {
+
+// Morton codes, sort, binary tree (PLOC clustering, or the Karras radix tree
+// when quality is kBvhFast) and the bottom-up pass (boxes, SAH costs, leaf
+// collapse with at most max_leaf items).  Item boxes in s.lo/hi and centroid
+// bounds in s.cbounds must be ready.
+cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t st, int quality) {
     morton_kernel<<<blocks(n), 256, 0, st>>>(s.lo, s.hi, n, s.cbounds, s.morton_in, s.idx_in);
     CK(cudaGetLastError());
     CK(cub::DeviceRadixSort::SortPairs(s.cub_tmp, s.cub_bytes, s.morton_in, s.morton, s.idx_in, s.idx, (int)n, 0,
                                        30, st));
     if (n > 1) {
-        karras_kernel<<<blocks(n - 1), 256, 0, st>>>(s.morton, (int)n, s.left, s.right, s.parent_i, s.parent_l,
-                                                    s.range_lo, s.range_hi);
-        CK(cudaGetLastError());
+        if (quality == kBvhPloc) {
+            CK(ploc_tree(s, n, st));
+        } else {
+            karras_kernel<<<blocks(n - 1), 256, 0, st>>>(s.morton, (int)n, s.left, s.right, s.parent_i, s.parent_l,
+                                                        s.range_lo, s.range_hi);
+            CK(cudaGetLastError());
+        }
         CK(cudaMemsetAsync(s.arrive, 0, (n - 1) * sizeof(uint32_t), st));
         bottom_up_kernel<<<blocks(n), 256, 0, st>>>((int)n, s.idx, s.lo, s.hi, s.left, s.right, s.parent_i,
                                                    s.parent_l, s.range_lo, s.range_hi, s.ilo, s.ihi, s.cost,
@@ -364,8 +380,8 @@ cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t s
 
 // Common tail: radix tree with leaves of up to kMaxLeaf items, emit BNode2.
 cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_base, uint32_t tri_base,
-                         BvhResult* res, cudaStream_t st) {
-    CK(radix_tree(s, n, kMaxLeaf, st));
+                         BvhResult* res, cudaStream_t st, int quality) {
+    CK(radix_tree(s, n, kMaxLeaf, st, quality));
     if (n > 1) {
         emit_nodes_kernel<<<blocks(n - 1), 256, 0, st>>>((int)n, s.idx, s.lo, s.hi, s.left, s.right, s.range_lo,
                                                         s.range_hi, s.ilo, s.ihi, s.collapse, nodes, node_base,
@@ -396,7 +412,8 @@ cudaError_t build_common(Scratch& s, uint32_t n, BNode2* nodes, uint32_t node_ba
 
 cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
-                               uint32_t tri_base, BvhResult* res, cudaStream_t st, const DevInstance* inst) {
+                               uint32_t tri_base, BvhResult* res, cudaStream_t st, const DevInstance* inst,
+                               int quality) {
     if (n == 0) return cudaErrorInvalidValue;
     Scratch s;
     cudaError_t e = scratch_alloc(s, n, st);
@@ -408,7 +425,7 @@ cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indi
                                                     s.cbounds, inst);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
+    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st, quality);
     if (e == cudaSuccess) {
         gather_tris_kernel<<<blocks(n), 256, 0, st>>>(s.idx, n, unsorted, tris, tri_base);
         e = cudaGetLastError();
@@ -420,7 +437,7 @@ cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indi
 
 cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_t* ids, uint32_t n, BNode2* nodes,
                                uint32_t node_base, TriRec* tris, uint32_t tri_base, BvhResult* res,
-                               cudaStream_t st) {
+                               cudaStream_t st, int quality) {
     if (n == 0) return cudaErrorInvalidValue;
     Scratch s;
     cudaError_t e = scratch_alloc(s, n, st);
@@ -431,7 +448,7 @@ cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_
         box_centroid_bounds_kernel<<<blocks(n), 256, 0, st>>>(s.lo, s.hi, n, s.cbounds);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
+    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st, quality);
     if (e == cudaSuccess) {
         gather_inst_kernel<<<blocks(n), 256, 0, st>>>(s.idx, n, ids, tris, tri_base);
         e = cudaGetLastError();
@@ -524,7 +541,7 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& bs, const gbrt_vertex
     tri_boxes_kernel<<<blocks(n), 256, 0, st>>>(vertices, indices, prims, items, n, s.lo, s.hi, bs.unsorted,
                                                 s.cbounds, nullptr);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st);
+    if (e == cudaSuccess) e = build_common(s, n, nodes, node_base, tri_base, res, st, kBvhFast);  // no allocation
     if (e == cudaSuccess) {
         gather_tris_kernel<<<blocks(n), 256, 0, st>>>(s.idx, n, bs.unsorted, tris, tri_base);
         e = cudaGetLastError();

@@ -175,6 +175,11 @@ struct BvhResult {
     float4 lo, hi;  // root bounds
 };
 
+// Binary-tree construction of the BVH builders: kBvhPloc clusters the items
+// (parallel locally-ordered clustering, better trees, a host wait per
+// round), kBvhFast splits the Morton order (Karras radix tree, one launch).
+constexpr int kBvhFast = 0, kBvhPloc = 1;
+
 // Item descriptors for triangle BVHs: x = instance id (world BVH) or 0,
 // y = BLAS geometry id, z = primitive id, w = opaque flag.
 // inst (may be null): items whose instance is not an identity one are
@@ -182,7 +187,7 @@ struct BvhResult {
 cudaError_t build_triangle_bvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                const uint4* items, uint32_t n, BNode2* nodes, uint32_t node_base, TriRec* tris,
                                uint32_t tri_base, BvhResult* result_host, cudaStream_t st,
-                               const DevInstance* inst = nullptr);
+                               const DevInstance* inst = nullptr, int quality = kBvhPloc);
 
 // Scratch of one triangle-BVH build supplied by the caller instead of being
 // allocated (every pointer 256-byte aligned, sized for `capacity` items).
@@ -218,7 +223,7 @@ cudaError_t build_triangle_bvh_scratch(const BuildScratch& scratch, const gbrt_v
 cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  const uint4* items, uint32_t n, CwNode* nodes, TriRec* tris, uint32_t* nodes_used,
                                  cudaStream_t st, std::vector<uint32_t>* level_starts = nullptr,
-                                 const DevInstance* inst = nullptr, int width = 8);
+                                 const DevInstance* inst = nullptr, int width = 8, int quality = kBvhPloc);
 // Refit of an 8-wide BVH built by build_triangle_cwbvh over the same
 // triangles: triangle records re-read from the vertices, then every node's
 // grid and child boxes recomputed level by level (level_starts: first node
@@ -232,7 +237,7 @@ cudaError_t refit_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* in
 // the instance ids.
 cudaError_t build_instance_bvh(const float4* lo, const float4* hi, const uint32_t* inst_ids, uint32_t n,
                                BNode2* nodes, uint32_t node_base, TriRec* tris, uint32_t tri_base,
-                               BvhResult* result_host, cudaStream_t st);
+                               BvhResult* result_host, cudaStream_t st, int quality = kBvhPloc);
 
 // Refit: recomputes every inner-node box of a triangle BVH bottom-up from the
 // current vertex positions, keeping the topology (used after skinning).

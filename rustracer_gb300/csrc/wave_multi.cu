@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_extend(WfState st,
     const uint32_t own = MultiWave{}.block_job(0), nj = c_wave.njobs;
     for (uint32_t t = 0; t < nj; ++t) extend_body<kMode>(MultiWave{}, st, b, own + t < nj ? own + t : own + t - nj);
 }
-__global__ void __launch_bounds__(128) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
+__global__ void __launch_bounds__(kShadeThreads) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_shadow(WfState st, uint32_t b) {
     const uint32_t own = MultiWave{}.block_job(2), nj = c_wave.njobs;
@@ -97,7 +97,7 @@ cudaError_t grids(Grid& g) {
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wfm_extend<kTraceWide>, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wfm_shade, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wfm_shade, kShadeThreads, 0)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wfm_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
@@ -208,7 +208,7 @@ cudaError_t enqueue_wave(const WfState& st, int mode, uint32_t nb, cudaStream_t 
         else wfm_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(st, b);
         te();
         tb(1);
-        wfm_shade<<<g_grid.shade, 128, 0, stream>>>(st, b);
+        wfm_shade<<<g_grid.shade, kShadeThreads, 0, stream>>>(st, b);
         te();
         tb(2);
         if (mode == kTraceWide) wfm_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(st, b);

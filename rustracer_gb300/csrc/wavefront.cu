@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
     wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     extend_body<kMode>(w, st, b, 0u);
 }
-__global__ void __launch_bounds__(128) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
+__global__ void __launch_bounds__(kShadeThreads) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     shade_body(w, st, b);
 }
 template <int kMode>
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleW
 
 // Radiance-cache forms of shade and finish, and the step that adds
 // throughput x cache output to the paths that stopped at bounce b.
-__global__ void __launch_bounds__(128) wf_shade_nrc(const __grid_constant__ SingleWave w, WfState st, uint32_t b,
+__global__ void __launch_bounds__(kShadeThreads) wf_shade_nrc(const __grid_constant__ SingleWave w, WfState st, uint32_t b,
                                                     const __grid_constant__ NrcWave nrc) {
     shade_body<SingleWave, true>(w, st, b, &nrc);
 }
@@ -109,7 +109,7 @@ cudaError_t grids(Grid& g) {
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend<kTraceWide>, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade, 128, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade, kShadeThreads, 0)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
@@ -230,8 +230,8 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 te();
                 if (side && b > 0 && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
                 tb(1);
-                if (nrc) wf_shade_nrc<<<g_grid.shade, 128, 0, stream>>>(w, st, b, *nrc);
-                else wf_shade<<<g_grid.shade, 128, 0, stream>>>(w, st, b);
+                if (nrc) wf_shade_nrc<<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b, *nrc);
+                else wf_shade<<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b);
                 te();
                 if (nrc && b >= 1 && !nrc->disabled) {  // cache queries of the paths that stopped here
                     tb(3);

@@ -31,7 +31,16 @@
 // with 4 or 6).
 constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 
+#ifndef GBRT_SORT_SHADOW
+#define GBRT_SORT_SHADOW 0
+#endif
+#ifndef GBRT_SHADE_THREADS
+#define GBRT_SHADE_THREADS 128
+#endif
+
 namespace gbrt {
+
+constexpr int kShadeThreads = GBRT_SHADE_THREADS;  // block size of the shade kernels
 
 GB_D uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -323,7 +332,12 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             no[slot] = f4(nxt_o, 0.0f);
             nd[slot] = f4(nxt_d, __uint_as_float(word));
         }
+#if GBRT_SORT_SHADOW
+        const uint32_t sslot = sort_rays ? block_append_by_key(&cnt[kShadow + b], shadow, octant_of(sd), s_key)
+                                         : warp_append(&cnt[kShadow + b], shadow);
+#else
         const uint32_t sslot = warp_append(&cnt[kShadow + b], shadow);
+#endif
         if (shadow) {
             st.sh_o[R + sslot] = f4(so, stmax);
             st.sh_d[R + sslot] = f4(sd, __uint_as_float(word));
