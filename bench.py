@@ -435,7 +435,7 @@ def run_batched(args):
             "autotune": {"seconds": round(t_tune, 3),
                          "chosen_width": {str(w): sum(t["chosen_width"] == w for t in tuned) for w in (2, 4, 8)},
                          "sort_rays": sum(t["sort_rays"] for t in tuned),
-                         "probe": "640x360, 2 spp, binary / 4-wide / 8-wide, then the ray-sort key; best of 2 after a warm-up"},
+                         "probe": "640x360, 2 spp, binary / 4-wide / 8-wide, each with the ray-sort key off and on; best of 2 after a warm-up"},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * 324,
                     "d2h_bytes_per_step": int(sum(w * h * 4 for _, w, h, _ in specs))},
             "clocks": clocks}

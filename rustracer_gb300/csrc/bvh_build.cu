@@ -21,7 +21,10 @@ namespace gbrt {
 
 namespace {
 
-constexpr float kCostTraverse = 1.2f;  // SAH cost of an inner node relative to one triangle test
+#ifndef GBRT_SAH_TRAVERSE
+#define GBRT_SAH_TRAVERSE 1.2f
+#endif
+constexpr float kCostTraverse = GBRT_SAH_TRAVERSE;  // SAH cost of an inner node relative to one triangle test
 constexpr float kCostTri = 1.0f;
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {

@@ -31,11 +31,14 @@
 // with 4 or 6).
 constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 
+// With the ray-sort key, shadow rays are grouped by octant too; shade blocks
+// of 256 threads make the groups twice as long (icosphere frame: 3719 Mrays/s
+// with neither, 3748 with both).
 #ifndef GBRT_SORT_SHADOW
-#define GBRT_SORT_SHADOW 0
+#define GBRT_SORT_SHADOW 1
 #endif
 #ifndef GBRT_SHADE_THREADS
-#define GBRT_SHADE_THREADS 128
+#define GBRT_SHADE_THREADS 256
 #endif
 
 namespace gbrt {
