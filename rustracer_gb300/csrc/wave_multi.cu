@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_extend(WfState st,
     const uint32_t own = MultiWave{}.block_job(0), nj = c_wave.njobs;
     for (uint32_t t = 0; t < nj; ++t) extend_body<kMode>(MultiWave{}, st, b, own + t < nj ? own + t : own + t - nj);
 }
-__global__ void __launch_bounds__(kShadeThreads) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
+__global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) wfm_shade(WfState st, uint32_t b) { shade_body(MultiWave{}, st, b); }
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode)) wfm_shadow(WfState st, uint32_t b) {
     const uint32_t own = MultiWave{}.block_job(2), nj = c_wave.njobs;

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
     wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     extend_body<kMode>(w, st, b, 0u);
 }
-__global__ void __launch_bounds__(kShadeThreads) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
+__global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     shade_body(w, st, b);
 }
 template <int kMode>
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) wf_finish(const __grid_constant__ SingleW
 
 // Radiance-cache forms of shade and finish, and the step that adds
 // throughput x cache output to the paths that stopped at bounce b.
-__global__ void __launch_bounds__(kShadeThreads) wf_shade_nrc(const __grid_constant__ SingleWave w, WfState st, uint32_t b,
+__global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) wf_shade_nrc(const __grid_constant__ SingleWave w, WfState st, uint32_t b,
                                                     const __grid_constant__ NrcWave nrc) {
     shade_body<SingleWave, true>(w, st, b, &nrc);
 }

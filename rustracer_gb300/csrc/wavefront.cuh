@@ -43,7 +43,15 @@ constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 
 namespace gbrt {
 
+// 2 blocks of 256: at most 128 registers, no spills.  Sweep on the icosphere
+// frame: (256, 2) 3768 Mrays/s; (256, 3) 3677 and (128, 6) 3659 with 80
+// registers and spills; (256, 1) let ptxas take more registers, one block per
+// SM, 3010.
+#ifndef GBRT_SHADE_MINB
+#define GBRT_SHADE_MINB 2
+#endif
 constexpr int kShadeThreads = GBRT_SHADE_THREADS;  // block size of the shade kernels
+constexpr int kShadeMinBlocks = GBRT_SHADE_MINB;   // resident blocks per SM the shade kernels are compiled for
 
 GB_D uint32_t lane_id() { return threadIdx.x & 31u; }
 
