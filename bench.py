@@ -548,6 +548,8 @@ def run_nrc(args):
     sd = WL.city_scene()
     ctx = gbrt.Context(0)
     sc = gbrt.Scene(ctx, sd)
+    # traversal layout and ray-sort key for this scene (untimed setup, on a plain 4-spp frame)
+    tuning = sc.autotune(sd.ubo(Wn, Hn, samples=4, bounces=depth, exposure=1.0, has_sky=True), Wn, Hn)
     ref_acc = gbrt.Accum(ctx, Wn, Hn)
     chunk = 32
     for k in range(0, args.ref_spp, chunk):
@@ -611,7 +613,8 @@ def run_nrc(args):
                        "cache": {"levels": 16, "table": 1 << 19, "features": 2, "mlp": "32-64x5-3 ReLU",
                                  "spp_per_frame": args.nrc_spp, "train_samples_per_frame": args.nrc_samples,
                                  "adam_steps_per_frame": args.nrc_steps, "lr": 1e-3,
-                                 "min_roughness": args.nrc_min_roughness}},
+                                 "min_roughness": args.nrc_min_roughness},
+                       "tuning": {"chosen_width": tuning["chosen_width"], "sort_rays": tuning["sort_rays"]}},
             "plain_pt": {"time_s": None if t_pt is None else t_pt / 1e3, "curve": pts_pt[:: max(1, len(pts_pt) // 24)],
                          "mrays_per_s": rays_pt / tot_pt / 1e3},
             "cache": {"time_s": None if t_nrc is None else t_nrc / 1e3,

@@ -494,9 +494,11 @@ int gbrt_scene_set_tuning(gbrt_scene* scene, uint32_t width, uint32_t sort_rays)
 #define GBRT_JOB_DONE     2u
 #define GBRT_JOB_POLICY_SRPT 0u
 #define GBRT_JOB_POLICY_FIFO 1u
-/* OR into the policy: on a deep queue waves grow to 2^26 paths instead of
- * 2^24 (throughput over latency).  Set it before the context's first submit:
- * the wave buffers (216 B per path) are sized then. */
+/* OR into the policy for throughput over latency: on a deep queue waves grow
+ * to 2^26 paths instead of 2^24, and a job of at least 2^24 paths runs alone
+ * through the single-frame kernels when its turn comes (it fills the GPU by
+ * itself).  Set it before the context's first submit: the wave buffers
+ * (216 B per path) are sized then. */
 #define GBRT_JOB_LARGE_WAVES 0x100u
 
 typedef struct gbrt_job_desc {

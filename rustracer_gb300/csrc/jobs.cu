@@ -46,6 +46,11 @@ double now_ms() {
 constexpr uint32_t kWaveCap = kMaxWavePaths < (1u << 22) ? kMaxWavePaths : (1u << 22);
 constexpr uint32_t kWaveCapDeep = kMaxWavePaths < (1u << 24) ? kMaxWavePaths : (1u << 24);
 constexpr uint32_t kWaveCapLarge = kMaxWavePaths < (1u << 26) ? kMaxWavePaths : (1u << 26);
+// With GBRT_JOB_LARGE_WAVES, a job of at least this many paths that no wave
+// has touched runs alone, through the single-frame kernels (a frame this
+// large fills the GPU by itself; the batched form's job table and partition
+// cost it about 5%)
+constexpr uint64_t kSoloPaths = 1ull << 24;
 constexpr uint32_t kChunkDiv = 8;             // pixel chunk = wave / 8 (finer packing)
 constexpr int kMaxInFlight = 2;
 
@@ -126,12 +131,20 @@ struct JobQueue {
     bool admit_one(std::unique_lock<std::mutex>& lk);
     int pack_and_launch();
     int run_cache_job(Job* j, std::unique_lock<std::mutex>& lk);
+    int run_solo_job(Job* j);
+    bool solo(const Job* j) const {
+        return deep_cap == kWaveCapLarge && j->paths_left >= kSoloPaths && j->paths_left == (uint64_t)j->npix * j->ns;
+    }
     int launch_next(std::unique_lock<std::mutex>& lk);
     void retire(Wave& w);
     void fail_active(int code, const std::string& msg);
 };
 
 namespace {
+
+// The binary traversal form (the wave kernels' kTraceBinary): chosen by the
+// autotuner, or the only one a world BVH without its 8-wide copy has.
+bool binary_traversal(const DevScene& s) { return s.prefer_binary || (s.has_world && !s.cw_nodes); }
 
 uint32_t scene_active(const JobQueue& q, const gbrt_scene* s) {
     uint32_t n = 0;
@@ -204,7 +217,7 @@ bool JobQueue::admit_one(std::unique_lock<std::mutex>& lk) {
 int JobQueue::pack_and_launch() {
     std::vector<Job*> order;
     for (Job* j : active)
-        if (j->paths_left && !j->cache) order.push_back(j);
+        if (j->paths_left && !j->cache && !solo(j)) order.push_back(j);
     if (order.empty()) return 1;
     if (policy == GBRT_JOB_POLICY_SRPT)
         std::stable_sort(order.begin(), order.end(),
@@ -223,8 +236,13 @@ int JobQueue::pack_and_launch() {
     for (const Job* j : order) queued += j->paths_left;
     const uint32_t cap = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(queued / 4, kWaveCap), deep_cap);
     uint32_t room = std::min(cap, ctx->wf.cap);
+    // a wave runs one traversal form for all its jobs: it packs only the jobs
+    // whose scenes traverse like the first one's (binary, or 8-wide with or
+    // without a TLAS), so a scene tuned for one form never runs in the other
+    const bool binary0 = binary_traversal(order.front()->scene->view);
     for (Job* j : order) {
         if (w->njobs == (uint32_t)kMaxWaveJobs || w->nsegs == (uint32_t)kMaxWaveSegs || room == 0) break;
+        if (binary_traversal(j->scene->view) != binary0) continue;
         const uint32_t slot = w->njobs, path0 = w->npaths;
         while (j->paths_left && room && w->nsegs < (uint32_t)kMaxWaveSegs) {
             const uint32_t npw = std::min(j->chunk, j->npix - j->px0);
@@ -342,6 +360,42 @@ int JobQueue::run_cache_job(Job* j, std::unique_lock<std::mutex>& lk) {
     return GBRT_OK;
 }
 
+// Renders a large untouched job alone with the single-frame kernels, like
+// gbrt_render_ex, and queues its completion like a wave's.  Lock held (no
+// host wait: the frame is only enqueued).
+int JobQueue::run_solo_job(Job* j) {
+    j->paths_left = 0;
+    RenderOut out{};
+    out.width = j->acc->w;
+    out.height = j->acc->h;
+    out.accum = j->acc->buf.as<float4>();
+    out.rgba8 = j->out_rgba8 ? j->img.as<uchar4>() : nullptr;
+    out.counters = j->counters.as<DeviceCounters>();
+    WfState wf = ctx->wf;
+    wf.frame_sum = j->frame_sum.as<float4>();
+    cudaError_t e = launch_wavefront(j->scene->view, j->ubo, out, wf, ctx->stream, nullptr, nullptr, nullptr, &ctx->side);
+    Wave wv;
+    if (e == cudaSuccess && free_events.empty()) {
+        cudaEvent_t ev;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) free_events.push_back(ev);
+    }
+    if (e == cudaSuccess) {
+        wv.ev = free_events.back();
+        free_events.pop_back();
+        e = cudaEventRecord(wv.ev, ctx->stream);
+        if (e != cudaSuccess) free_events.push_back(wv.ev);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail_active(GBRT_E_CUDA, std::string("solo job launch: ") + cudaGetErrorString(e));
+        return GBRT_E_CUDA;
+    }
+    wv.finishing.push_back(j);
+    inflight.push_back(std::move(wv));
+    return GBRT_OK;
+}
+
 // Launches the next unit of work: a cache job when one comes first in the
 // policy's order, else a batched wave of the other jobs.  Returns GBRT_OK,
 // or 1 when no active job has paths left.  Lock held.
@@ -357,7 +411,12 @@ int JobQueue::launch_next(std::unique_lock<std::mutex>& lk) {
     }
     if (!first) return 1;
     if (first->cache) return run_cache_job(first, lk);
-    return pack_and_launch();
+    if (solo(first)) return run_solo_job(first);
+    const int rc = pack_and_launch();
+    if (rc != 1) return rc;
+    for (Job* j : active)  // only solo jobs left
+        if (j->paths_left && solo(j)) return run_solo_job(j);
+    return 1;
 }
 
 // A wave's event has fired: finish the jobs it completed.  Lock held.
