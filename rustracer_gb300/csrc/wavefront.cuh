@@ -22,13 +22,14 @@
 #include "persistent.cuh"
 
 // Resident 128-thread blocks per SM the traversal kernels (extend, shadow)
-// are compiled for: 5 gives them 96 registers, enough to keep the traversal
-// state and the 8-wide node decode out of local memory, at 20 warps per SM.
+// are compiled for: 7 gives them 72 registers (a few dozen bytes of spills)
+// at 28 warps per SM.  The traversal waits on dependent node loads, so warps
+// pay more than registers: on the icosphere frame with the clustered BVH,
+// 4 / 5 / 6 / 7 / 8 blocks gave 3472 / 3768 / 4046 / 4159 / 4134 Mrays/s.
 #ifndef GBRT_TRACE_MINB
-#define GBRT_TRACE_MINB 5
+#define GBRT_TRACE_MINB 7
 #endif
-// Same bound for every traversal form (the TLAS form measured no faster
-// with 4 or 6).
+// Same bound for every traversal form.
 constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 
 // With the ray-sort key, shadow rays are grouped by octant too; shade blocks
