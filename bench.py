@@ -183,18 +183,19 @@ def common_line(args, n, value, ms_per_step, extra_cfg=None):
             "config": cfg}
 
 
-def traffic_from_profile(kernel, rays_per_launch):
-    """DRAM bytes (read + write) per launch of `kernel`: the per-ray figure of
-    the committed ncu capture (profiles/dram_traffic_icosphere7.json, a
-    smaller case of this workload) times the rays of one launch here (null
-    when that kernel has no capture)."""
+def traffic_from_profile(kernel, units_per_launch):
+    """DRAM bytes (read + write) of one launch of `kernel`: the per-unit
+    traffic of an ncu capture of that kernel on a small case of this workload
+    (profiles/dram_traffic_icosphere7.json; units: rays for the traversal
+    kernels, shaded hits for shade) times the units of a full launch, or None
+    when that kernel has no capture."""
     p = os.path.join(ROOT, "profiles", "dram_traffic_icosphere7.json")
     if not os.path.exists(p):
         return None
     d = json.load(open(p)).get(kernel)
-    if not d or not rays_per_launch:
+    if not d or not units_per_launch:
         return None
-    return d["dram_bytes_per_ray"] * rays_per_launch
+    return d["dram_bytes_per_unit"] * units_per_launch
 
 
 def run_gpu(args):
@@ -310,8 +311,9 @@ def run_gpu(args):
     max_wave = 1 << 26  # paths per single-frame wave (the library's kMaxWavePaths)
     waves = -(-(W * H * SPP) // min(W * H * SPP, max_wave))
     stage_launches = waves * DEPTH * stage_frames
-    rays_per_launch = (stage_rays[0] if kernel_name == "wf_extend" else stage_rays[2]) / max(stage_launches, 1)
-    traffic = traffic_from_profile(kernel_name, rays_per_launch)
+    # units of one launch of the dominant kernel: rays (extend, shadow) or shaded hits (shade)
+    units = {"wf_extend": stage_rays[0], "wf_shade": shaded, "wf_shadow": stage_rays[2]}.get(kernel_name, 0)
+    traffic = traffic_from_profile(kernel_name, units / max(stage_launches, 1))
     line = common_line(args, world, value, dev_ms / args.steps,
                        {"kernel": args.mode, "wall_ms_per_step": wall / args.steps * 1e3,
                         "launches_per_step": launches,
