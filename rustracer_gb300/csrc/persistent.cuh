@@ -19,7 +19,12 @@
 namespace gbrt {
 
 constexpr int kEmpty = 0x7FFFFFFF;  // "stack exhausted"
-constexpr uint32_t kRefill = 8;     // idle lanes that trigger a refill
+// icosphere frame (8-wide, clustered BVH, 7 blocks per SM): 4 / 8 / 12 / 16 /
+// 20 / 24 idle lanes gave 4034 / 4174 / 4225 / 4288 / 4262 / 4183 Mrays/s
+#ifndef GBRT_REFILL
+#define GBRT_REFILL 16
+#endif
+constexpr uint32_t kRefill = GBRT_REFILL;  // idle lanes that trigger a refill
 
 // Loader: bool load(uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx)
 // Finisher: void finish(uint32_t q, bool hit, const Hit& h)

@@ -35,9 +35,6 @@ constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 // With the ray-sort key, shadow rays are grouped by octant too; shade blocks
 // of 256 threads make the groups twice as long (icosphere frame: 3719 Mrays/s
 // with neither, 3748 with both).
-#ifndef GBRT_SORT_SHADOW
-#define GBRT_SORT_SHADOW 1
-#endif
 #ifndef GBRT_SHADE_THREADS
 #define GBRT_SHADE_THREADS 256
 #endif
@@ -66,32 +63,39 @@ GB_D uint32_t warp_append(uint32_t* counter, bool want) {
     return base + __popc(mask & ((1u << lane_id()) - 1u));
 }
 
-// Block-wide queue append grouped by a 3-bit key (the ray's direction
-// octant): the block's wanted entries get one contiguous range of the queue,
-// key 0 first, so a warp that later takes consecutive entries sees rays of
-// few octants.  Order within a key is unspecified (every consumer indexes
-// path state by the path id the entry carries).  Every thread of the block
-// calls it; s: 17 words of shared memory.
-GB_D uint32_t block_append_by_key(uint32_t* counter, bool want, uint32_t key, uint32_t* s) {
-    if (threadIdx.x < 8) s[threadIdx.x] = 0;
-    __syncthreads();
+// Block-wide appends to two queues (the extension and the shadow queue)
+// grouped by a 3-bit key (the ray's direction octant): each queue gets one
+// contiguous range per block, key 0 first, so a warp that later takes
+// consecutive entries sees rays of few octants.  Order within a key is
+// unspecified (every consumer indexes path state by the path id the entry
+// carries).  Every thread of the block calls it; s: 34 words of shared memory.
+GB_D uint32_t group_rank(bool want, uint32_t key, uint32_t* bins) {
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, want ? key : 8u);
-    uint32_t base = 0;
     const uint32_t leader = __ffs(peers) - 1u;
-    if (want && lane_id() == leader) base = atomicAdd(&s[key], (uint32_t)__popc(peers));
+    uint32_t base = 0;
+    if (want && lane_id() == leader) base = atomicAdd(&bins[key], (uint32_t)__popc(peers));
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    const uint32_t rank = base + __popc(peers & ((1u << lane_id()) - 1u));
+    return base + __popc(peers & ((1u << lane_id()) - 1u));
+}
+
+GB_D void block_append2_by_key(uint32_t* counter_a, bool want_a, uint32_t key_a, uint32_t* counter_b, bool want_b,
+                               uint32_t key_b, uint32_t* s, uint32_t& slot_a, uint32_t& slot_b) {
+    if (threadIdx.x < 16) s[threadIdx.x] = 0;  // [0, 8): queue a's bins, [8, 16): queue b's
     __syncthreads();
-    if (threadIdx.x == 0) {
+    const uint32_t ra = group_rank(want_a, key_a, s), rb = group_rank(want_b, key_b, s + 8);
+    __syncthreads();
+    if (threadIdx.x < 2) {  // thread 0: queue a, thread 1: queue b
+        const uint32_t q = threadIdx.x;
         uint32_t tot = 0;
         for (int k = 0; k < 8; ++k) {
-            s[8 + k] = tot;
-            tot += s[k];
+            s[16 + 8 * q + k] = tot;
+            tot += s[8 * q + k];
         }
-        s[16] = tot ? atomicAdd(counter, tot) : 0u;
+        s[32 + q] = tot ? atomicAdd(q ? counter_b : counter_a, tot) : 0u;
     }
     __syncthreads();
-    return want ? s[16] + s[8 + key] + rank : 0u;
+    slot_a = want_a ? s[32] + s[16 + key_a] + ra : 0u;
+    slot_b = want_b ? s[33] + s[24 + key_b] + rb : 0u;
 }
 
 GB_D uint32_t octant_of(float3 d) { return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u); }
@@ -245,8 +249,8 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
     const uint32_t blk0 = w.blk0(1, jb), nblk = w.nblk(1, jb);
     const uint32_t stride = nblk * blockDim.x;
     const bool sort_rays = s.sort_rays != 0u;
-    __shared__ uint32_t s_key[17];
-    // block-uniform trip count (block_append_by_key synchronises the block)
+    __shared__ uint32_t s_key[34];
+    // block-uniform trip count (block_append2_by_key synchronises the block)
     for (uint32_t cbase = (blockIdx.x - blk0) * blockDim.x; cbase < n; cbase += stride) {
         const uint32_t q = cbase + threadIdx.x;
         const bool active = q < n;
@@ -338,18 +342,18 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             nxt_d = Rp.scatterDir;
             }
         }
-        const uint32_t slot = sort_rays ? block_append_by_key(&cnt[kQueue + b + 1], cont, octant_of(nxt_d), s_key)
-                                        : warp_append(&cnt[kQueue + b + 1], cont);
+        uint32_t slot, sslot;
+        if (sort_rays) {
+            block_append2_by_key(&cnt[kQueue + b + 1], cont, octant_of(nxt_d), &cnt[kShadow + b], shadow,
+                                 octant_of(sd), s_key, slot, sslot);
+        } else {
+            slot = warp_append(&cnt[kQueue + b + 1], cont);
+            sslot = warp_append(&cnt[kShadow + b], shadow);
+        }
         if (cont) {
             no[slot] = f4(nxt_o, 0.0f);
             nd[slot] = f4(nxt_d, __uint_as_float(word));
         }
-#if GBRT_SORT_SHADOW
-        const uint32_t sslot = sort_rays ? block_append_by_key(&cnt[kShadow + b], shadow, octant_of(sd), s_key)
-                                         : warp_append(&cnt[kShadow + b], shadow);
-#else
-        const uint32_t sslot = warp_append(&cnt[kShadow + b], shadow);
-#endif
         if (shadow) {
             st.sh_o[R + sslot] = f4(so, stmax);
             st.sh_d[R + sslot] = f4(sd, __uint_as_float(word));
