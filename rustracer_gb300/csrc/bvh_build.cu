@@ -365,9 +365,9 @@ cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t s
     CK(cub::DeviceRadixSort::SortPairs(s.cub_tmp, s.cub_bytes, s.morton_in, s.morton, s.idx_in, s.idx, (int)n, 0,
                                        30, st));
     if (n > 1) {
-        if (quality == kBvhPloc) {
-            CK(ploc_tree(s, n, st));
-        } else {
+        cudaError_t pe = quality == kBvhPloc ? ploc_tree(s, n, st) : cudaErrorNotReady;
+        if (pe != cudaSuccess && pe != cudaErrorNotReady) return pe;
+        if (pe == cudaErrorNotReady) {  // radix tree (asked for, or clustering did not converge)
             karras_kernel<<<blocks(n - 1), 256, 0, st>>>(s.morton, (int)n, s.left, s.right, s.parent_i, s.parent_l,
                                                         s.range_lo, s.range_hi);
             CK(cudaGetLastError());

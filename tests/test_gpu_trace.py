@@ -143,3 +143,41 @@ def test_icosphere_rays_match(gpu_ctx):
     hits, st = gbrt.Scene(gpu_ctx, sd).trace(rays)
     assert_hits_equal(hits, ref)
     assert st["device_status"] == 0
+
+
+@pytest.mark.parametrize("layout", ["coincident", "grid"])
+def test_degenerate_layouts_build_and_match(gpu_ctx, layout):
+    """Boxes that tie under the clustering's merge cost: 30,000 copies of one
+    triangle (every ray hitting one of them ties in t, so the smallest
+    primitive must win) and a regular 200 x 150 grid of equal triangles.  The
+    build converges (the clustering pairs tied neighbours) and every hit is
+    the oracle's."""
+    from rustracer_gb300 import gbrt
+    from rustracer_gb300.scenes import GeoBuilder, random_pbr_material
+    rng = np.random.default_rng(5)
+    b = GeoBuilder()
+    mat = b.add_material(random_pbr_material(rng))
+    if layout == "coincident":
+        n = 30000
+        tri = np.array([[-0.5, -0.5, 0.0], [0.5, -0.5, 0.0], [0.0, 0.6, 0.0]])
+        p = np.tile(tri, (n, 1))
+    else:
+        xs, ys = np.meshgrid(np.arange(200), np.arange(150))
+        o = np.stack([xs.ravel(), ys.ravel(), np.zeros(xs.size)], 1) * 0.01 - np.array([1.0, 0.75, 0.0])
+        p = (o[:, None, :] + np.array([[0.0, 0.0, 0.0], [0.01, 0.0, 0.0], [0.0, 0.01, 0.0]])[None]).reshape(-1, 3)
+        n = len(o)
+    nrm = np.tile([[0.0, 0.0, 1.0]], (3 * n, 1))
+    vb = b.add_vertices(p.astype(np.float32), nrm.astype(np.float32))
+    b.add_geometry(vb, 3 * n, np.arange(3 * n).reshape(-1, 3), mat)
+    sd = b.finish(camera=dict(eye=(0, 0, 3.0), direction=(0, 0, -1), fov_deg=60.0), name=f"degenerate_{layout}")
+    sc = gbrt.Scene(gpu_ctx, sd)
+    rays = np.zeros(4096, T.RAY)
+    rays["org"] = np.column_stack([rng.uniform(-1, 1, 4096), rng.uniform(-0.8, 0.8, 4096), np.full(4096, 2.0)])
+    rays["dir"] = np.tile([0.0, 0.0, -1.0], (4096, 1))
+    rays["tmin"] = 0.0
+    rays["tmax"] = 1e4
+    hits, st = sc.trace(rays)
+    ref, _ = oracle_scene(sd).trace(rays)
+    assert_hits_equal(hits, ref)
+    assert st["device_status"] == 0
+    assert (hits["instance_id"] != 0xFFFFFFFF).sum() > 100
