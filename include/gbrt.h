@@ -257,9 +257,17 @@ typedef struct gbrt_stats {
 #define GBRT_MODE_MEGAKERNEL 1
 #define GBRT_MODE_WAVEFRONT  2
 #define GBRT_RENDER_STAGE_TIMING 0x1u  /* gbrt_render_opts.flags: CUDA-event time per stage */
+/* gbrt_render_opts.flags: queue the frame on the context stream and return
+ * at once (the non-blocking form of gbrt_render).  out_rgba8, if given, is
+ * written when the stream reaches the frame: keep it valid and read it after
+ * gbrt_sync (page-locked memory lets the copy run asynchronously; a pageable
+ * buffer makes this call wait for it).  stats gets only kernel_launches; the
+ * debug outputs and stage timing are not available.  gbrt_sync reports a
+ * traversal limit hit by any asynchronous frame since the last gbrt_sync. */
+#define GBRT_RENDER_ASYNC 0x2u
 typedef struct gbrt_render_opts {
     uint32_t mode;            /* GBRT_MODE_* */
-    uint32_t flags;           /* GBRT_RENDER_STAGE_TIMING or 0 */
+    uint32_t flags;           /* GBRT_RENDER_STAGE_TIMING, GBRT_RENDER_ASYNC or 0 */
     /* Optional debug outputs (host memory, may be NULL):
      * sample_radiance: width*height*number_of_samples*3 floats, per-sample
      *                  path radiance, laid out [pixel][sample][rgb];
@@ -288,7 +296,9 @@ int gbrt_ctx_destroy(gbrt_ctx* ctx);
 const char* gbrt_last_error(const gbrt_ctx* ctx);
 /* Free / total device memory as seen by this context. */
 int gbrt_ctx_mem_info(gbrt_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
-/* Waits for all work queued on the context's stream. */
+/* Waits for all work queued on the context's stream; returns
+ * GBRT_E_DEVICE_LIMIT if a frame queued with GBRT_RENDER_ASYNC since the
+ * last gbrt_sync hit a traversal limit. */
 int gbrt_sync(gbrt_ctx* ctx);
 /* Library version string, e.g. "gbrt 0.1 sm_103a". */
 const char* gbrt_version(void);

@@ -121,6 +121,8 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
 
 int cw_width(const gbrt_scene* s) { return (s->build_flags & GBRT_BUILD_WIDTH4) ? 4 : 8; }
 
+__global__ void or_status_kernel(const DeviceCounters* dc, uint32_t* acc) { *acc |= dc->status; }
+
 void refresh_view(gbrt_scene* s) {
     DevScene& v = s->view;
     v.nodes = s->nodes.as<BNode2>();
@@ -482,6 +484,15 @@ int gbrt_sync(gbrt_ctx* c) {
     if (!c) return fail(c, GBRT_E_INVALID, "NULL context");
     DeviceGuard g(c->device);
     CU(c, cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (c->async_status.p) {
+        uint32_t status = 0;
+        CU(c, cudaMemcpy(&status, c->async_status.p, 4, cudaMemcpyDeviceToHost), "download status");
+        if (status) {
+            CU(c, cudaMemset(c->async_status.p, 0, 4), "memset");
+            return fail(c, GBRT_E_DEVICE_LIMIT, "an asynchronous frame reported a traversal limit (status " +
+                                                    std::to_string(status) + ")");
+        }
+    }
     return GBRT_OK;
 }
 
@@ -696,6 +707,9 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     if (ubo->number_of_samples == 0 || ubo->total_number_of_samples < ubo->number_of_samples)
         return fail(c, GBRT_E_INVALID, "need 0 < number_of_samples <= total_number_of_samples");
     if (opts && opts->mode > GBRT_MODE_WAVEFRONT) return fail(c, GBRT_E_INVALID, "unknown render mode");
+    const bool async = opts && (opts->flags & GBRT_RENDER_ASYNC);
+    if (async && (opts->sample_radiance || opts->primary_hits || (opts->flags & GBRT_RENDER_STAGE_TIMING)))
+        return fail(c, GBRT_E_INVALID, "asynchronous frames have no debug outputs or stage timing");
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
     const uint32_t W = acc->w, H = acc->h, ns = ubo->number_of_samples;
@@ -738,6 +752,19 @@ int gbrt_render_ex(gbrt_scene* s, const gbrt_ubo* ubo, gbrt_accum* acc, uint8_t*
     }
     CU(c, cudaEventRecord(c->ev1, st), "event");
     if (out_rgba8) CU(c, cudaMemcpyAsync(out_rgba8, out.rgba8, npix * 4, cudaMemcpyDeviceToHost, st), "download image");
+    if (async) {  // the frame's status joins the context's; gbrt_sync reads it
+        if (!c->async_status.p) {
+            CU(c, c->async_status.alloc(4), "cudaMalloc(status)");
+            CU(c, cudaMemsetAsync(c->async_status.p, 0, 4, st), "memset");
+        }
+        or_status_kernel<<<1, 1, 0, st>>>(out.counters, c->async_status.as<uint32_t>());
+        CU(c, cudaGetLastError(), "status launch");
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            stats->kernel_launches = launches;
+        }
+        return GBRT_OK;
+    }
     if (out.sample_radiance)
         CU(c, cudaMemcpyAsync(opts->sample_radiance, out.sample_radiance, npix * ns * 3 * sizeof(float),
                               cudaMemcpyDeviceToHost, st),

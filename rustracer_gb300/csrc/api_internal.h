@@ -55,6 +55,7 @@ struct gbrt_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, tb0 = nullptr, tb1 = nullptr;
     std::string err;
     gbrt_host::DevBuf counters;
+    gbrt_host::DevBuf async_status;  // OR of the status words of frames rendered with GBRT_RENDER_ASYNC
     gbrt_host::DevBuf trace_work;  // fetch cursor of the persistent ray-query kernel
     gbrt_host::DevBuf scratch_rays, scratch_hits, scratch_img, scratch_samples, scratch_phits;
     gbrt_host::DevBuf wf_mem, wf_frame;  // wavefront queues / path state, per-pixel frame sums

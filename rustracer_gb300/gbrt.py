@@ -26,6 +26,7 @@ OK, E_INVALID, E_CUDA, E_OOM, E_DEVICE_LIMIT, E_NOT_BUILT, E_NO_DEVICE, E_BUSY =
 BUILD_NO_FLATTEN = 0x1
 BUILD_WIDTH4 = 0x2
 MODE_AUTO, MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1, 2
+RENDER_STAGE_TIMING, RENDER_ASYNC = 0x1, 0x2
 
 # name -> (restype, argtypes); every symbol include/gbrt.h declares
 P, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
@@ -398,18 +399,21 @@ class Scene:
         """gbrt_scene_set_tuning: BVH width 2/4/8 and the ray-sort key, set directly."""
         self.ctx.check(self.ctx.L.gbrt_scene_set_tuning(self.h, width, int(bool(sort_rays))))
 
-    def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False):
+    def render(self, ubo, accum, image=True, mode=MODE_AUTO, want_samples=False, want_hits=False,
+               asynchronous=False, out=None):
         """One frame (record_raytracing_commands + the shaders).  Returns a dict
         with 'image' (HxWx4 uint8 or None), 'stats', and the optional
-        per-sample radiance [pixel][sample][3] and primary hits."""
+        per-sample radiance [pixel][sample][3] and primary hits.  With
+        asynchronous=True the frame is only queued (GBRT_RENDER_ASYNC): the
+        image (written into `out` when given) is valid after ctx.sync()."""
         ubo = np.asarray(ubo, T.UBO).reshape(())
         W, H = accum.w, accum.h_
         ns = int(ubo["number_of_samples"])
-        img = np.zeros((H, W, 4), np.uint8) if image else None
+        img = (out if out is not None else np.zeros((H, W, 4), np.uint8)) if image else None
         st = np.zeros((), T.STATS)
         samples = np.zeros((H * W, ns, 3), np.float32) if want_samples else None
         hits = np.zeros((H * W, ns), T.HIT) if want_hits else None
-        opts = RenderOpts(mode, 0, samples.ctypes.data if want_samples else None,
+        opts = RenderOpts(mode, RENDER_ASYNC if asynchronous else 0, samples.ctypes.data if want_samples else None,
                           hits.ctypes.data if want_hits else None)
         self.ctx.check(self.ctx.L.gbrt_render_ex(self.h, _p(ubo), accum.h, _p(img), _p(st), C.byref(opts)))
         return dict(image=img, stats=st, samples=samples, hits=hits)

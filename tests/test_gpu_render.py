@@ -153,3 +153,25 @@ def test_wavefront_pixel_chunks(gpu_ctx):
     ok = np.all(np.abs(x - y) <= 1e-4 * np.maximum(np.abs(x), np.abs(y)) + 1e-6, axis=-1)
     assert ok.mean() > 1 - FLIP_MAX
     assert int(ra["stats"]["rays_camera"]) == int(rb["stats"]["rays_camera"]) == W * H
+
+
+def test_async_frames_equal_sync(gpu_ctx):
+    """Four frames queued with GBRT_RENDER_ASYNC, then gbrt_sync: the same
+    accumulation and last image as four synchronous frames."""
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=3)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    W, H = 200, 120
+    ubos = [sd.ubo(W, H, samples=2, total=2 * (f + 1), bounces=6, exposure=1.0) for f in range(4)]
+    a_sync, a_async = gbrt.Accum(gpu_ctx, W, H), gbrt.Accum(gpu_ctx, W, H)
+    for u in ubos:
+        img_sync = sc.render(u, a_sync)["image"]
+    out = np.zeros((H, W, 4), np.uint8)
+    for u in ubos:
+        r = sc.render(u, a_async, asynchronous=True, out=out)
+        assert r["stats"]["kernel_launches"] > 0
+    gpu_ctx.sync()
+    assert np.array_equal(out, img_sync)
+    assert np.array_equal(a_async.download(), a_sync.download())
+    with pytest.raises(gbrt.GbrtError):  # no debug outputs on the asynchronous form
+        sc.render(ubos[0], a_async, asynchronous=True, want_samples=True)
