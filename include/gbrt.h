@@ -197,6 +197,7 @@ typedef struct gbrt_geo_range {
 #define GBRT_TEX_RGBA8_UNORM 0
 #define GBRT_TEX_RGBA8_SRGB  1
 #define GBRT_TEX_RGBA16F     2
+#define GBRT_TEX_RGBA32F     3  /* linear float texels (HDR skyboxes; no reference counterpart) */
 #define GBRT_WRAP_REPEAT          0
 #define GBRT_WRAP_CLAMP_TO_EDGE   1
 #define GBRT_WRAP_MIRRORED_REPEAT 2
@@ -367,6 +368,10 @@ int gbrt_lights_set(gbrt_scene* scene,
 /* Skybox cubemap: 6 square RGBA8 (sRGB-encoded) faces of face_size^2 texels
  * in the order +X,-X,+Y,-Y,+Z,-Z (globals.rs:175-199).  NULL clears it. */
 int gbrt_skybox_set(gbrt_scene* scene, uint32_t face_size, const uint8_t* rgba8_faces);
+/* The same with the texel format given: GBRT_TEX_RGBA8_SRGB (as
+ * gbrt_skybox_set) or GBRT_TEX_RGBA32F (linear floats, 16 B per texel, for
+ * HDR environment maps). */
+int gbrt_skybox_set_ex(gbrt_scene* scene, uint32_t face_size, const void* faces, uint32_t format);
 
 /* ------------------------------------------------------------------------ */
 /* Accumulation image                                                       */

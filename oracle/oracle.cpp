@@ -547,6 +547,11 @@ int wrap_index(int i, int n, uint32_t mode) {
 
 vec4 fetch(const Texture& t, int x, int y) {
     size_t k = (size_t)y * t.w + (size_t)x;
+    if (t.format == GBRT_TEX_RGBA32F) {
+        float f[4];
+        std::memcpy(f, t.data.data() + 16 * k, 16);
+        return vec4(f[0], f[1], f[2], f[3]);
+    }
     if (t.format == GBRT_TEX_RGBA16F) {
         const uint16_t* p = reinterpret_cast<const uint16_t*>(t.data.data()) + 4 * k;
         return vec4(half_to_float(p[0]), half_to_float(p[1]), half_to_float(p[2]), half_to_float(p[3]));
@@ -1586,7 +1591,7 @@ orc_scene* orc_scene_create(const gbrt_vertex* v, uint32_t nv, const uint32_t* i
         t.format = tex[i].format;
         t.wrap_s = tex[i].wrap_s;
         t.wrap_t = tex[i].wrap_t;
-        size_t bytes = (size_t)t.w * t.h * (t.format == GBRT_TEX_RGBA16F ? 8 : 4);
+        size_t bytes = (size_t)t.w * t.h * (t.format == GBRT_TEX_RGBA32F ? 16 : t.format == GBRT_TEX_RGBA16F ? 8 : 4);
         if (tex[i].data && bytes) {
             const uint8_t* p = static_cast<const uint8_t*>(tex[i].data);
             t.data.assign(p, p + bytes);
@@ -1642,15 +1647,23 @@ int orc_lights_set(orc_scene* s, const gbrt_light_raw* d, uint32_t nd, const gbr
 }
 
 int orc_skybox_set(orc_scene* s, uint32_t face_size, const uint8_t* faces) {
+    return orc_skybox_set_ex(s, face_size, faces, GBRT_TEX_RGBA8_SRGB);
+}
+
+// Cube faces as RGBA8 sRGB (the reference's decoded JPEG faces) or linear
+// RGBA32F (an HDR extension of the GB300 library).
+int orc_skybox_set_ex(orc_scene* s, uint32_t face_size, const void* faces_v, uint32_t format) {
+    if (format != GBRT_TEX_RGBA8_SRGB && format != GBRT_TEX_RGBA32F) return GBRT_E_INVALID;
+    const uint8_t* faces = static_cast<const uint8_t*>(faces_v);
     s->sky_size = faces ? face_size : 0;
     s->sky_faces.clear();
     if (!faces) return GBRT_OK;
-    size_t fb = (size_t)face_size * face_size * 4;
+    size_t fb = (size_t)face_size * face_size * (format == GBRT_TEX_RGBA32F ? 16 : 4);
     s->sky_faces.resize(6);
     for (int f = 0; f < 6; ++f) {
         Texture& t = s->sky_faces[f];
         t.w = t.h = face_size;
-        t.format = GBRT_TEX_RGBA8_SRGB;
+        t.format = format;
         t.wrap_s = t.wrap_t = GBRT_WRAP_CLAMP_TO_EDGE;
         t.data.assign(faces + f * fb, faces + (f + 1) * fb);
     }

@@ -43,6 +43,7 @@ int  orc_build_flags(orc_scene* s, uint32_t flags);
 int  orc_lights_set(orc_scene* s, const gbrt_light_raw* d, uint32_t nd,
                     const gbrt_light_raw* p, uint32_t np);
 int  orc_skybox_set(orc_scene* s, uint32_t face_size, const uint8_t* rgba8_faces);
+int  orc_skybox_set_ex(orc_scene* s, uint32_t face_size, const void* faces, uint32_t format);
 /* Skins vertices like AnimationCompute.comp and rebuilds the BVHs. */
 int  orc_skin(orc_scene* s, const gbrt_skin_raw* skins, uint32_t nskin);
 /* Copies the (possibly skinned) vertex buffer out. */

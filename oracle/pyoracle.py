@@ -38,6 +38,7 @@ def lib():
         L.orc_build_flags.argtypes = [P, u32]
         L.orc_lights_set.argtypes = [P, P, u32, P, u32]
         L.orc_skybox_set.argtypes = [P, u32, P]
+        L.orc_skybox_set_ex.argtypes = [P, u32, P, u32]
         L.orc_skin.argtypes = [P, P, u32]
         L.orc_get_vertices.argtypes = [P, P, u32]
         L.orc_trace.argtypes = [P, P, u32, u32, P, i32, i32, P]
@@ -100,8 +101,12 @@ class OracleScene:
         assert L.orc_lights_set(self.h, _p(sd.dlights), len(sd.dlights), _p(sd.plights), len(sd.plights)) == 0
         if sd.skybox is not None:
             size, faces = sd.skybox
-            faces = np.ascontiguousarray(faces, np.uint8)
-            assert L.orc_skybox_set(self.h, size, _p(faces)) == 0
+            if np.asarray(faces).dtype == np.float32:  # linear RGBA32F faces
+                faces = np.ascontiguousarray(faces, np.float32)
+                assert L.orc_skybox_set_ex(self.h, size, _p(faces), 3) == 0
+            else:
+                faces = np.ascontiguousarray(faces, np.uint8)
+                assert L.orc_skybox_set(self.h, size, _p(faces)) == 0
 
     def __del__(self):
         if getattr(self, "h", None):

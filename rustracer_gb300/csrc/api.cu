@@ -123,6 +123,10 @@ int cw_width(const gbrt_scene* s) { return (s->build_flags & GBRT_BUILD_WIDTH4) 
 
 __global__ void or_status_kernel(const DeviceCounters* dc, uint32_t* acc) { *acc |= dc->status; }
 
+size_t texel_bytes(uint32_t format) {
+    return format == GBRT_TEX_RGBA32F ? 16u : format == GBRT_TEX_RGBA16F ? 8u : 4u;
+}
+
 void refresh_view(gbrt_scene* s) {
     DevScene& v = s->view;
     v.nodes = s->nodes.as<BNode2>();
@@ -139,8 +143,9 @@ void refresh_view(gbrt_scene* s) {
     v.nd = s->nd;
     v.plights = s->plights.as<gbrt_light_raw>();
     v.np = s->np;
-    v.sky = s->sky.as<uchar4>();
+    v.sky = s->sky.p;
     v.sky_size = s->sky_size;
+    v.sky_format = s->sky_format;
     v.cw_nodes = s->cw_count ? s->cw_nodes.as<CwNode>() : nullptr;
     v.cw_tris = s->cw_count ? s->cw_tris.as<TriRec>() : nullptr;
     v.blas_cw_nodes = s->blas_cw_nodes.p ? s->blas_cw_nodes.as<CwNode>() : nullptr;
@@ -534,11 +539,11 @@ int gbrt_scene_create(gbrt_ctx* c, const gbrt_vertex* v, uint32_t nv, const uint
     for (uint32_t i = 0; i < ntex; ++i) {
         const gbrt_texture_desc& t = tex[i];
         std::memset(&dt[i], 0, sizeof(DevTexture));
-        if (t.format > GBRT_TEX_RGBA16F || t.wrap_s > 2 || t.wrap_t > 2) {
+        if (t.format > GBRT_TEX_RGBA32F || t.wrap_s > 2 || t.wrap_t > 2) {
             delete s;
             return fail(c, GBRT_E_INVALID, "texture " + std::to_string(i) + ": bad format or wrap mode");
         }
-        const size_t bytes = (size_t)t.width * t.height * (t.format == GBRT_TEX_RGBA16F ? 8 : 4);
+        const size_t bytes = (size_t)t.width * t.height * texel_bytes(t.format);
         DevBuf* b = new DevBuf();
         s->tex_data.push_back(b);
         if (bytes && t.data) {
@@ -634,18 +639,26 @@ int gbrt_lights_set(gbrt_scene* s, const gbrt_light_raw* d, uint32_t nd, const g
 }
 
 int gbrt_skybox_set(gbrt_scene* s, uint32_t size, const uint8_t* faces) {
+    return gbrt_skybox_set_ex(s, size, faces, GBRT_TEX_RGBA8_SRGB);
+}
+
+int gbrt_skybox_set_ex(gbrt_scene* s, uint32_t size, const void* faces, uint32_t format) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    if (format != GBRT_TEX_RGBA8_SRGB && format != GBRT_TEX_RGBA32F)
+        return fail(c, GBRT_E_INVALID, "skybox format must be GBRT_TEX_RGBA8_SRGB or GBRT_TEX_RGBA32F");
     if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     DeviceGuard g(c->device);
     if (!faces || size == 0) {
         s->sky.release();
         s->sky_size = 0;
     } else {
-        CU(c, upload(s->sky, faces, (size_t)size * size * 4 * 6, c->stream), "upload(skybox)");
+        const size_t bytes = (size_t)size * size * texel_bytes(format) * 6;
+        CU(c, upload(s->sky, static_cast<const uint8_t*>(faces), bytes, c->stream), "upload(skybox)");
         CU(c, cudaStreamSynchronize(c->stream), "sync");
         s->sky_size = size;
     }
+    s->sky_format = format;
     refresh_view(s);
     return GBRT_OK;
 }

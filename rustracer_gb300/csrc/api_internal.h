@@ -79,7 +79,7 @@ struct gbrt_scene {
     std::vector<gbrt_geo_range> ranges;  // by geo id
     std::vector<uint8_t> has_range;
     std::vector<gbrt_instance> instances;
-    uint32_t nd = 0, np = 0, sky_size = 0;
+    uint32_t nd = 0, np = 0, sky_size = 0, sky_format = GBRT_TEX_RGBA8_SRGB;
     bool skinned = false;
     bool all_opaque = true;
     // acceleration structures

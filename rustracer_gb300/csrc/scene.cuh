@@ -102,8 +102,9 @@ struct DevScene {
     uint32_t nd;
     const gbrt_light_raw* plights;
     uint32_t np;
-    const uchar4* sky;   // 6 faces, size^2 each
+    const void* sky;     // 6 faces, size^2 texels each
     uint32_t sky_size;
+    uint32_t sky_format; // GBRT_TEX_RGBA8_SRGB or GBRT_TEX_RGBA32F
     uint32_t all_opaque; // every geometry is OPAQUE: the any-hit test never runs
     uint32_t prefer_binary;  // autotuner's choice: traverse the binary layout even where 8-wide nodes exist
     uint32_t sort_rays;      // autotuner's choice: shade writes each block's extension rays grouped by octant

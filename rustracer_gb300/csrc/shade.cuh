@@ -373,6 +373,7 @@ GB_D int wrap_idx(int i, int n, uint32_t mode) {
 GB_D float half_bits_to_float(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 GB_D float4 tex_fetch(const DevTexture& t, int x, int y) {
     size_t k = (size_t)y * t.w + (size_t)x;
+    if (t.format == GBRT_TEX_RGBA32F) return __ldg(reinterpret_cast<const float4*>(t.data) + k);
     if (t.format == GBRT_TEX_RGBA16F) {
         uint2 raw = __ldg(reinterpret_cast<const uint2*>(t.data) + k);
         return f4(half_bits_to_float(raw.x & 0xFFFF), half_bits_to_float(raw.x >> 16),
@@ -426,9 +427,10 @@ GB_D float3 sample_sky(const DevScene& s, float3 d) {
         if (d.z >= 0.0f) { face = 4; sc = d.x; tc = -d.y; } else { face = 5; sc = -d.x; tc = -d.y; }
     }
     DevTexture t;
-    t.data = s.sky + (size_t)face * s.sky_size * s.sky_size;
+    const size_t texel = s.sky_format == GBRT_TEX_RGBA32F ? 16u : 4u;
+    t.data = static_cast<const unsigned char*>(s.sky) + (size_t)face * s.sky_size * s.sky_size * texel;
     t.w = t.h = s.sky_size;
-    t.format = GBRT_TEX_RGBA8_SRGB;
+    t.format = s.sky_format;
     t.wrap_s = t.wrap_t = GBRT_WRAP_CLAMP_TO_EDGE;
     float4 r = sample_tex2d(t, 0.5f * (sc / ma + 1.0f), 0.5f * (tc / ma + 1.0f));
     return f3(r.x, r.y, r.z);

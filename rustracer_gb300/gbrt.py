@@ -45,6 +45,7 @@ SIGNATURES = {
     "gbrt_skin_and_refit": (i32, [P, P, u32]),
     "gbrt_lights_set": (i32, [P, P, u32, P, u32]),
     "gbrt_skybox_set": (i32, [P, u32, P]),
+    "gbrt_skybox_set_ex": (i32, [P, u32, P, u32]),
     "gbrt_accum_create": (i32, [P, u32, u32, C.POINTER(P)]),
     "gbrt_accum_reset": (i32, [P]),
     "gbrt_accum_download": (i32, [P, P]),
@@ -381,6 +382,11 @@ class Scene:
         self.ctx.check(self.ctx.L.gbrt_lights_set(self.h, _p(d), len(d), _p(p), len(p)))
 
     def set_skybox(self, size, faces):
+        """6 faces of size^2 texels: uint8 RGBA (sRGB) or float32 RGBA (linear, HDR)."""
+        if faces is not None and np.asarray(faces).dtype == np.float32:
+            faces = np.ascontiguousarray(faces, np.float32)
+            self.ctx.check(self.ctx.L.gbrt_skybox_set_ex(self.h, size, _p(faces), T.TEX_RGBA32F))
+            return
         faces = None if faces is None else np.ascontiguousarray(faces, np.uint8)
         self.ctx.check(self.ctx.L.gbrt_skybox_set(self.h, size, _p(faces)))
 

@@ -81,7 +81,7 @@ assert MATERIAL.fields["specular_texture"][1] == 160
 assert MATERIAL.fields["sg_diffuse_factor"][1] == 208
 
 # Texture formats / wrap modes (include/gbrt.h)
-TEX_RGBA8_UNORM, TEX_RGBA8_SRGB, TEX_RGBA16F = 0, 1, 2
+TEX_RGBA8_UNORM, TEX_RGBA8_SRGB, TEX_RGBA16F, TEX_RGBA32F = 0, 1, 2, 3
 WRAP_REPEAT, WRAP_CLAMP_TO_EDGE, WRAP_MIRRORED_REPEAT = 0, 1, 2
 
 # Ray flags

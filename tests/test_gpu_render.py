@@ -175,3 +175,17 @@ def test_async_frames_equal_sync(gpu_ctx):
     assert np.array_equal(a_async.download(), a_sync.download())
     with pytest.raises(gbrt.GbrtError):  # no debug outputs on the asynchronous form
         sc.render(ubos[0], a_async, asynchronous=True, want_samples=True)
+
+
+def test_hdr_float_skybox(gpu_ctx):
+    """An RGBA32F (linear, HDR: texels up to 20) skybox through
+    gbrt_skybox_set_ex: per-sample radiance matches the oracle's."""
+    import pyoracle as O
+    sd = scenes.icosphere_scene(subdiv=2)
+    rng = np.random.default_rng(4)
+    sd.skybox = (8, (rng.random(6 * 8 * 8 * 4) * 20.0).astype(np.float32))
+    ubo = sd.ubo(64, 48, samples=4, bounces=6, exposure=1.0, has_sky=True, eye=(0.3, 0.2, 3.8),
+                 direction=(0.3, 0.1, -1.0))
+    ref = O.OracleScene(sd).render(ubo, 64, 48, want_samples=True)
+    r = render_gpu(gpu_ctx, sd, ubo, 64, 48)
+    assert compare_samples(r["samples"], ref["samples"]) <= FLIP_MAX * 5

@@ -264,3 +264,29 @@ def test_accumulation_semantics():
     o.render(sd.ubo(16, 16, samples=4, total=4, bounces=4), 16, 16, accum=acc2)
     assert np.allclose(acc, acc2, rtol=1e-5, atol=1e-7)
     assert not np.array_equal(first, acc)
+
+
+def test_float_skybox_equals_decoded_srgb():
+    """RGBA32F sky faces holding the sRGB-decoded values of RGBA8 faces render
+    the same miss radiance (same bilinear math, linear texels)."""
+    import ctypes as C
+    import pyoracle as O
+    from rustracer_gb300 import scenes
+    rng = np.random.default_rng(8)
+    faces8 = rng.integers(0, 256, 6 * 8 * 8 * 4).astype(np.uint8)
+    lut = np.array([((c / 255.0) / 12.92) if c / 255.0 <= 0.04045 else (((c / 255.0) + 0.055) / 1.055) ** 2.4
+                    for c in range(256)], np.float64)
+    dirs = rng.normal(size=(200, 3)).astype(np.float32)
+    out = []
+    for faces in (faces8, None):
+        sd = scenes.cornell()
+        if faces is None:  # linear floats: decoded colour, alpha / 255
+            f = faces8.reshape(-1, 4).astype(np.float64)
+            faces = np.column_stack([lut[faces8.reshape(-1, 4)[:, :3]], f[:, 3] / 255.0]).astype(np.float32)
+        sd.skybox = (8, faces)
+        o = O.OracleScene(sd)
+        res = np.zeros((len(dirs), 3), np.float32)
+        for i, d in enumerate(dirs):
+            O.lib().orc_sample_skybox(o.h, d.ctypes.data_as(C.c_void_p), res[i].ctypes.data_as(C.c_void_p))
+        out.append(res)
+    assert np.allclose(out[0], out[1], rtol=2e-6, atol=1e-7)
