@@ -467,6 +467,22 @@ typedef struct gbrt_tune_report {
 } gbrt_tune_report;
 int gbrt_scene_autotune(gbrt_scene* scene, const gbrt_ubo* probe_ubo, uint32_t width, uint32_t height,
                         gbrt_tune_report* report);
+/* BVH figures of a scene.  gbrt_skin_and_refit refits the wide world BVH in
+ * place (topology kept); once its SAH cost proxy has grown 1.3x over the
+ * built tree's, the refit turns into a full rebuild. */
+typedef struct gbrt_scene_info {
+    uint32_t world_triangles;  /* triangles in the world BVH (flattened instances included) */
+    uint32_t wide_nodes;       /* nodes of the wide world BVH */
+    uint32_t wide_width;       /* 4 or 8 */
+    uint32_t refits;           /* refits since the last full build */
+    uint32_t drift_rebuilds;   /* full rebuilds forced by refit drift */
+    uint32_t _pad;
+    double sah_built;          /* SAH cost proxy of the wide world BVH as built: summed child-box area
+                                  over the root box's (0 when there is no wide world BVH) */
+    double sah_now;            /* the same after the last refit */
+} gbrt_scene_info;
+int gbrt_scene_info_get(gbrt_scene* scene, gbrt_scene_info* info);
+
 /* Sets the autotuner's two choices directly: BVH width 2 (binary), 4 or 8
  * (rebuilding the wide BVHs when the width changes) and the ray-sort key
  * (sort_rays != 0).  Synchronous. */

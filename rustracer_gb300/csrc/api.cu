@@ -33,6 +33,7 @@ static_assert(sizeof(gbrt_stats) == 104, "stats record");
 static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 64, "job records");
 static_assert(sizeof(gbrt_nrc_config) == 56 && sizeof(gbrt_nrc_render_opts) == 16, "cache records");
 static_assert(sizeof(gbrt_tune_report) == 40, "tune report");
+static_assert(sizeof(gbrt_scene_info) == 40, "scene info");
 
 namespace {
 thread_local std::string g_create_error;
@@ -253,6 +254,19 @@ int build_all(gbrt_scene* s) {
                                    &s->cw_levels, s->inst.as<DevInstance>(), cw_width(s)),
            "build wide world BVH");
         s->nworld = (uint32_t)nw;
+        // the tree's SAH cost proxy as built (a refit of unchanged vertices rewrites the same nodes), the
+        // reference for the drift check of later refits
+        s->cw_sah0 = 0.0;
+        s->refits = 0;
+        if (s->cw_levels.size() >= 2) {
+            CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4) + 16), "cudaMalloc(refit boxes)");
+            CU(c, refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                       s->prims.as<gbrt_priminfo>(), s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(),
+                                       s->nworld, s->cw_levels, s->cw_boxes.as<float4>(), st,
+                                       s->inst.as<DevInstance>(), &s->cw_sah0),
+               "measure wide world BVH");
+            s->cw_sah = s->cw_sah0;
+        }
     } else {
         s->cw_nodes.release();
         s->cw_tris.release();
@@ -369,6 +383,8 @@ int skin_scene(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin) {
     return refit_world(s);
 }
 
+constexpr double kRefitDrift = 1.3;
+
 int refit_world(gbrt_scene* s) {
     gbrt_ctx* c = s->ctx;
     DevScene& v = s->view;
@@ -382,12 +398,20 @@ int refit_world(gbrt_scene* s) {
                              s->items.as<uint4>(), s->nworld, s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r,
                              st, s->inst.as<DevInstance>(), kBvhFast),
        "rebuild world BVH");
-    CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4)), "cudaMalloc(refit boxes)");
+    CU(c, s->cw_boxes.reserve((size_t)s->cw_count * 2 * sizeof(float4) + 16), "cudaMalloc(refit boxes)");
+    double sah = 0.0;
     CU(c, refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(), s->prims.as<gbrt_priminfo>(),
                                s->cw_nodes.as<CwNode>(), s->cw_tris.as<TriRec>(), s->nworld, s->cw_levels,
-                               s->cw_boxes.as<float4>(), st, s->inst.as<DevInstance>()),
+                               s->cw_boxes.as<float4>(), st, s->inst.as<DevInstance>(), &sah),
        "refit wide world BVH");
-    CU(c, cudaStreamSynchronize(st), "sync after refit");
+    ++s->refits;
+    s->cw_sah = sah;
+    // topology kept through large deformations loses quality: rebuild once the tree's SAH cost proxy has
+    // grown by kRefitDrift over the built tree's
+    if (s->cw_sah0 > 0.0 && sah > kRefitDrift * s->cw_sah0) {
+        ++s->rebuilds;
+        return build_all(s);
+    }
     v.world_root = r.root;
     v.world_lo = r.lo;
     v.world_hi = r.hi;
@@ -881,6 +905,20 @@ int gbrt_scene_autotune(gbrt_scene* s, const gbrt_ubo* ubo, uint32_t width, uint
         rep->chosen_width = best_l == 0 ? 2u : (uint32_t)cw_width(s);
         rep->sort_rays = s->view.sort_rays;
     }
+    return GBRT_OK;
+}
+
+int gbrt_scene_info_get(gbrt_scene* s, gbrt_scene_info* info) {
+    if (!s) return GBRT_E_INVALID;
+    if (!info) return fail(s->ctx, GBRT_E_INVALID, "NULL info");
+    std::memset(info, 0, sizeof(*info));
+    info->world_triangles = s->nworld;
+    info->wide_nodes = s->cw_count;
+    info->wide_width = (uint32_t)cw_width(s);
+    info->refits = s->refits;
+    info->drift_rebuilds = s->rebuilds;
+    info->sah_built = s->cw_sah0;
+    info->sah_now = s->cw_sah;
     return GBRT_OK;
 }
 

@@ -90,6 +90,9 @@ struct gbrt_scene {
     gbrt_host::DevBuf cw_boxes;        // refit scratch: float boxes of the 8-wide nodes
     uint32_t nworld = 0;               // triangles in the world BVH
     uint32_t build_flags = 0;          // gbrt_blas_build flags (GBRT_BUILD_NO_FLATTEN, GBRT_BUILD_WIDTH4)
+    double cw_sah0 = 0.0;              // SAH cost proxy of the 8-wide world BVH as built (refit drift reference)
+    double cw_sah = 0.0;               // ... after the last refit
+    uint32_t refits = 0, rebuilds = 0; // refits since the build; full rebuilds forced by refit drift
     uint32_t cw_count = 0;
     bool built = false;
     std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene

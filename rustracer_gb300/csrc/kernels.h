@@ -227,11 +227,15 @@ cudaError_t build_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* in
 // Refit of an 8-wide BVH built by build_triangle_cwbvh over the same
 // triangles: triangle records re-read from the vertices, then every node's
 // grid and child boxes recomputed level by level (level_starts: first node
-// of each level, last entry = node count).  boxes: 2 float4 per node scratch.
-// No host synchronisation.
+// of each level, last entry = node count).  boxes: scratch of 2 float4 per
+// node plus one float.  No host synchronisation unless sah_host is given: it
+// then gets the tree's SAH traversal cost proxy, the summed surface area of
+// every node's child boxes over the root box's (the expected child-box tests
+// of a ray through the root), after a host wait.
 cudaError_t refit_triangle_cwbvh(const gbrt_vertex* vertices, const uint32_t* indices, const gbrt_priminfo* prims,
                                  CwNode* nodes, TriRec* tris, uint32_t ntris, const std::vector<uint32_t>& level_starts,
-                                 float4* boxes, cudaStream_t st, const DevInstance* inst = nullptr);
+                                 float4* boxes, cudaStream_t st, const DevInstance* inst = nullptr,
+                                 double* sah_host = nullptr);
 
 // TLAS over instances: boxes given per instance (lo/hi), the leaf slots carry
 // the instance ids.

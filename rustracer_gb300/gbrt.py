@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbrt_render_nrc": (i32, [P, P, P, P, P, P, P, P]),
     "gbrt_scene_autotune": (i32, [P, P, u32, u32, P]),
     "gbrt_scene_set_tuning": (i32, [P, u32, u32]),
+    "gbrt_scene_info_get": (i32, [P, P]),
 }
 JOB_QUEUED, JOB_RUNNING, JOB_DONE = 0, 1, 2
 POLICY_SRPT, POLICY_FIFO = 0, 1
@@ -400,6 +401,14 @@ class Scene:
         u = rep[4:].view(np.uint32)
         return dict(ms_binary=float(rep[0]), ms_wide=float(rep[1]), ms_wide4=float(rep[2]),
                     ms_sorted=float(rep[3]), chosen_width=int(u[0]), sort_rays=int(u[1]))
+
+    def info(self):
+        """gbrt_scene_info_get: world BVH sizes, refit count, drift rebuilds and SAH cost proxies."""
+        raw = np.zeros(5, np.float64)
+        self.ctx.check(self.ctx.L.gbrt_scene_info_get(self.h, _p(raw)))
+        u = raw[:3].view(np.uint32)
+        return dict(world_triangles=int(u[0]), wide_nodes=int(u[1]), wide_width=int(u[2]), refits=int(u[3]),
+                    drift_rebuilds=int(u[4]), sah_built=float(raw[3]), sah_now=float(raw[4]))
 
     def set_tuning(self, width=8, sort_rays=False):
         """gbrt_scene_set_tuning: BVH width 2/4/8 and the ray-sort key, set directly."""

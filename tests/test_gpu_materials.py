@@ -108,3 +108,38 @@ def test_skinned_tube_render(gpu_ctx):
     r = sc.render(ubo, gbrt.Accum(gpu_ctx, 64, 64), want_samples=True, want_hits=True, mode=2)
     assert np.array_equal(r["hits"]["primitive_id"], ref["hits"]["primitive_id"])
     assert flip_share(r["samples"], ref["samples"]) <= 5e-3
+
+
+def test_refit_drift_triggers_rebuild(gpu_ctx):
+    """A mild bend refits the wide BVH in place (SAH cost proxy within 1.3x of
+    the built tree's); scattering the bones across the box makes the proxy
+    grow past that, so the refit becomes a full rebuild.  Hits match the
+    oracle's after both."""
+    import pyoracle as O
+    from rustracer_gb300 import gbrt
+    sd = zoo.skinned_tube()
+    rays = _tube_rays(sd)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    orc = O.OracleScene(sd)
+    info0 = sc.info()
+    assert info0["sah_built"] > 1.0 and info0["refits"] == 0 and info0["wide_nodes"] > 0
+    mild = zoo.bone_matrices(sd.bones, 0.7)
+    sc.skin_and_refit(mild)
+    info1 = sc.info()
+    assert info1["refits"] == 1 and info1["drift_rebuilds"] == 0
+    assert info1["sah_now"] < 1.3 * info1["sah_built"]
+    scatter = zoo.bone_matrices(sd.bones, 0.7)
+    for k in range(sd.bones):
+        M = scatter[0]["joints"][k].reshape(4, 4).T.copy()  # column-major storage
+        M[0, 3] += 0.85 * (1 if k % 2 == 0 else -1)
+        M[2, 3] += 0.85 * (1 if (k // 2) % 2 == 0 else -1)
+        scatter[0]["joints"][k] = M.T.reshape(16)
+    sc.skin_and_refit(scatter)
+    info2 = sc.info()
+    assert info2["drift_rebuilds"] == 1 and info2["refits"] == 0
+    orc.skin(scatter)
+    g, _ = sc.trace(rays)
+    o, _ = orc.trace(rays)
+    for f in ("instance_id", "primitive_id"):
+        assert np.array_equal(g[f], o[f]), f
+    assert np.array_equal(g["t"].view(np.uint32), o["t"].view(np.uint32))
