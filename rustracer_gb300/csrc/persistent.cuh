@@ -21,6 +21,13 @@ namespace gbrt {
 constexpr int kEmpty = 0x7FFFFFFF;  // "stack exhausted"
 // icosphere frame (8-wide, clustered BVH, 7 blocks per SM): 4 / 8 / 12 / 16 /
 // 20 / 24 idle lanes gave 4034 / 4174 / 4225 / 4288 / 4262 / 4183 Mrays/s
+// Entries of the 8-wide traversal stack kept in shared memory (0: the whole
+// stack in local memory, which stays in L1).  Icosphere frame: 4254 Mrays/s
+// with 0, 4258 with 8, 4256 with 16 (noise), so L1 keeps its capacity for
+// nodes and triangles.
+#ifndef GBRT_CW_SMEM_STACK
+#define GBRT_CW_SMEM_STACK 0
+#endif
 #ifndef GBRT_REFILL
 #define GBRT_REFILL 16
 #endif
@@ -183,7 +190,23 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
                               Loader&& load, Finisher&& finish) {
     const uint32_t lane = threadIdx.x & 31u;
     const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+#if GBRT_CW_SMEM_STACK
+    // the top kSmemStack entries of each lane's stack in shared memory ([entry][thread]: a warp's accesses
+    // to one depth are consecutive 8-byte words), deeper ones in local memory; every traversal kernel
+    // runs 128-thread blocks (its launch bound)
+    constexpr int kSmemStack = GBRT_CW_SMEM_STACK;
+    __shared__ uint2 s_stack[kSmemStack][128];
+    uint2 stack[kCwStack - kSmemStack];
+    auto push = [&](uint2 v, int i) {
+        if (i < kSmemStack) s_stack[i][threadIdx.x] = v;
+        else stack[i - kSmemStack] = v;
+    };
+    auto pop = [&](int i) { return i < kSmemStack ? s_stack[i][threadIdx.x] : stack[i - kSmemStack]; };
+#else
     uint2 stack[kCwStack];
+    auto push = [&](uint2 v, int i) { stack[i] = v; };
+    auto pop = [&](int i) { return stack[i]; };
+#endif
     bool has = false, exhausted = false;
     uint32_t q = 0, oct = 0;
     TRay r;
@@ -230,7 +253,7 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
         }
         if (!has) continue;
         bool done = false;
-        while (!(ng.y & 0xFF000000u) && sp > 0) ng = stack[--sp];
+        while (!(ng.y & 0xFF000000u) && sp > 0) ng = pop(--sp);
         if (!(ng.y & 0xFF000000u)) {
             done = true;
         } else if (++iter > kMaxIter) {
@@ -242,7 +265,7 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
             const uint32_t slot = (bit - 24u) ^ oct;
             const uint32_t child = ng.x + __popc((ng.y & 0xFFu) & ((1u << slot) - 1u));
             if (ng.y & 0xFF000000u) {
-                if (sp < kCwStack) stack[sp++] = ng;
+                if (sp < kCwStack) push(ng, sp++);
                 else ts.status |= GBRT_STATUS_STACK_OVERFLOW;
             }
             uint32_t cb, tb, im;
