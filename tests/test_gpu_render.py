@@ -189,3 +189,27 @@ def test_hdr_float_skybox(gpu_ctx):
     ref = O.OracleScene(sd).render(ubo, 64, 48, want_samples=True)
     r = render_gpu(gpu_ctx, sd, ubo, 64, 48)
     assert compare_samples(r["samples"], ref["samples"]) <= FLIP_MAX * 5
+
+
+def test_converged_vs_fp64_reference(gpu_ctx):
+    """Converged images: the GPU's FP32 render (16384 spp, samples 0..16383)
+    and the oracle's FP64-intersection render of other samples
+    (16384..32767) of the Cornell box agree to relMSE = mean((x - ref)^2 /
+    (ref^2 + 1e-2)) below 1e-2, the contract's convergence measure (two
+    independent estimates: about 3e-3 expected from their noise)."""
+    import pyoracle as O
+    from rustracer_gb300 import gbrt
+    sd = scenes.cornell()
+    W = H = 16
+    sc = gbrt.Scene(gpu_ctx, sd)
+    acc = gbrt.Accum(gpu_ctx, W, H)
+    N = 16384
+    sc.render(sd.ubo(W, H, samples=N, total=N, bounces=8, exposure=1.0), acc, image=False)
+    x = acc.download()[..., :3] / float(N)
+    ref_acc = np.zeros((H * W, 4), np.float32)
+    O.OracleScene(sd).render(sd.ubo(W, H, samples=N, total=2 * N, bounces=8, exposure=1.0), W, H,
+                             accum=ref_acc, fp64=True, out=False)
+    ref = ref_acc.reshape(H, W, 4)[..., :3] / float(N)
+    relmse = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+    assert np.isfinite(relmse) and relmse < 1e-2, relmse
+    assert ref.mean() > 0.05  # the box is lit
