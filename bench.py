@@ -550,8 +550,12 @@ def run_nrc(args):
     sd = WL.city_scene()
     ctx = gbrt.Context(0)
     sc = gbrt.Scene(ctx, sd)
-    # traversal layout and ray-sort key for this scene (untimed setup, on a plain 4-spp frame)
-    tuning = sc.autotune(sd.ubo(Wn, Hn, samples=4, bounces=depth, exposure=1.0, has_sky=True), Wn, Hn)
+    # traversal layout and ray-sort key for this scene (untimed setup, on a plain 4-spp frame), or fixed
+    if args.tune == "auto":
+        tuning = sc.autotune(sd.ubo(Wn, Hn, samples=4, bounces=depth, exposure=1.0, has_sky=True), Wn, Hn)
+    else:
+        tuning = {"chosen_width": int(args.tune[1]), "sort_rays": int(args.tune.endswith("s"))}
+        sc.set_tuning(tuning["chosen_width"], bool(tuning["sort_rays"]))
     ref_acc = gbrt.Accum(ctx, Wn, Hn)
     chunk = 32
     for k in range(0, args.ref_spp, chunk):
@@ -667,7 +671,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--res", default=None, help="WxH override for small profiling cases (default 1920x1080)")
     ap.add_argument("--tune", default="auto", choices=["auto", "w2", "w4", "w8", "w2s", "w4s", "w8s"],
-                    help="icosphere: autotuner (untimed setup) or a fixed BVH width w2/w4/w8, s = ray-sort key on")
+                    help="icosphere, nrc: autotuner (untimed setup) or a fixed BVH width w2/w4/w8, s = ray-sort key on")
     ap.add_argument("--spp", type=int, default=None, help="samples per step override (default 64)")
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched", "serving", "nrc"],
                     help="icosphere: the headline frame; batched: 32 scenes as one batch of jobs; "

@@ -119,6 +119,7 @@ constexpr size_t kInferSmem = (size_t)kBf16Padded * 2 + (size_t)kInferWarps * 32
 __global__ void __launch_bounds__(128) nrc_infer_kernel(NrcView v, const float4* __restrict__ q, uint32_t n,
                                                         float4* __restrict__ out, const uint32_t* n_dev) {
     if (n_dev) n = min(n, *n_dev);
+    if (blockIdx.x * kInferWarps * 32u >= n) return;  // no queries for this block: skip the weight copy
     extern __shared__ __align__(16) unsigned char smem[];
     __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(smem);
     __nv_bfloat16* sin_all = sw + kBf16Padded;
@@ -264,6 +265,7 @@ __global__ void __launch_bounds__(128, 1) nrc_infer_tc_kernel(NrcView v, const f
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sa + kTcRows * kNrcHidden * 2);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     if (n_dev) n = min(n, *n_dev);
+    if (blockIdx.x * kTcRows >= n) return;  // no tile for this block: skip the weight copy and the allocation
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     {  // weights are pre-arranged in core-matrix order by the host
         const uint4* src = reinterpret_cast<const uint4*>(wtc);
