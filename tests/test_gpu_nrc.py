@@ -54,7 +54,7 @@ def test_query_matches_oracle(gpu_ctx, flags, n):
     c.set_params(mlp, grid)
     pos = _points(rng, 5000)
     ref, _ = N.forward(mlp, grid, _p01(pos), N.level_table(BASE, GROWTH, LOG2T), LOG2T)
-    scale = np.abs(ref).max()  # of the 5000 points, so that n = 1 and 128 are judged on the same scale
+    scale = np.abs(ref).max()  # of the 5000 points, so that n = 1 and 128 are compared on the same scale
     y = c.query(pos[:n])
     err = np.abs(y - ref[:n])
     assert np.all(np.isfinite(y))
