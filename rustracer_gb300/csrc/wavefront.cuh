@@ -68,7 +68,10 @@ GB_D uint32_t warp_append(uint32_t* counter, bool want) {
 // contiguous range per block, key 0 first, so a warp that later takes
 // consecutive entries sees rays of few octants.  Order within a key is
 // unspecified (every consumer indexes path state by the path id the entry
-// carries).  Every thread of the block calls it; s: 34 words of shared memory.
+// carries).  Every thread of the block calls it.  Two barriers per call: the
+// 34-word work areas `cur` and `nxt` alternate between calls, and each call
+// clears the bins of the next one's area between its barriers (the caller
+// clears both before the first call).
 GB_D uint32_t group_rank(bool want, uint32_t key, uint32_t* bins) {
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, want ? key : 8u);
     const uint32_t leader = __ffs(peers) - 1u;
@@ -79,23 +82,24 @@ GB_D uint32_t group_rank(bool want, uint32_t key, uint32_t* bins) {
 }
 
 GB_D void block_append2_by_key(uint32_t* counter_a, bool want_a, uint32_t key_a, uint32_t* counter_b, bool want_b,
-                               uint32_t key_b, uint32_t* s, uint32_t& slot_a, uint32_t& slot_b) {
-    if (threadIdx.x < 16) s[threadIdx.x] = 0;  // [0, 8): queue a's bins, [8, 16): queue b's
-    __syncthreads();
-    const uint32_t ra = group_rank(want_a, key_a, s), rb = group_rank(want_b, key_b, s + 8);
+                               uint32_t key_b, uint32_t* cur, uint32_t* nxt, uint32_t& slot_a, uint32_t& slot_b) {
+    // cur: [0, 8) queue a's bins, [8, 16) queue b's, [16, 32) their offsets, [32, 34) their bases
+    const uint32_t ra = group_rank(want_a, key_a, cur), rb = group_rank(want_b, key_b, cur + 8);
     __syncthreads();
     if (threadIdx.x < 2) {  // thread 0: queue a, thread 1: queue b
         const uint32_t q = threadIdx.x;
         uint32_t tot = 0;
         for (int k = 0; k < 8; ++k) {
-            s[16 + 8 * q + k] = tot;
-            tot += s[8 * q + k];
+            cur[16 + 8 * q + k] = tot;
+            tot += cur[8 * q + k];
         }
-        s[32 + q] = tot ? atomicAdd(q ? counter_b : counter_a, tot) : 0u;
+        cur[32 + q] = tot ? atomicAdd(q ? counter_b : counter_a, tot) : 0u;
+    } else if (threadIdx.x < 18) {
+        nxt[threadIdx.x - 2] = 0;  // nobody reads nxt between the previous call's first barrier and here
     }
     __syncthreads();
-    slot_a = want_a ? s[32] + s[16 + key_a] + ra : 0u;
-    slot_b = want_b ? s[33] + s[24 + key_b] + rb : 0u;
+    slot_a = want_a ? cur[32] + cur[16 + key_a] + ra : 0u;
+    slot_b = want_b ? cur[33] + cur[24 + key_b] + rb : 0u;
 }
 
 GB_D uint32_t octant_of(float3 d) { return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u); }
@@ -249,7 +253,12 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
     const uint32_t blk0 = w.blk0(1, jb), nblk = w.nblk(1, jb);
     const uint32_t stride = nblk * blockDim.x;
     const bool sort_rays = s.sort_rays != 0u;
-    __shared__ uint32_t s_key[34];
+    __shared__ uint32_t s_key[2][34];
+    uint32_t parity = 0;
+    if (sort_rays) {  // block-uniform
+        if (threadIdx.x < 68) (&s_key[0][0])[threadIdx.x] = 0;
+        __syncthreads();
+    }
     // block-uniform trip count (block_append2_by_key synchronises the block)
     for (uint32_t cbase = (blockIdx.x - blk0) * blockDim.x; cbase < n; cbase += stride) {
         const uint32_t q = cbase + threadIdx.x;
@@ -345,7 +354,8 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         uint32_t slot, sslot;
         if (sort_rays) {
             block_append2_by_key(&cnt[kQueue + b + 1], cont, octant_of(nxt_d), &cnt[kShadow + b], shadow,
-                                 octant_of(sd), s_key, slot, sslot);
+                                 octant_of(sd), s_key[parity], s_key[parity ^ 1u], slot, sslot);
+            parity ^= 1u;
         } else {
             slot = warp_append(&cnt[kQueue + b + 1], cont);
             sslot = warp_append(&cnt[kShadow + b], shadow);
