@@ -102,7 +102,10 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
         w.ray_d[0] = (float4*)take(f4);
         w.ray_d[1] = (float4*)take(f4);
         w.hit = (float4*)take(f4);
-        w.path = (float4*)take(4 * f4);
+        w.tp = (float4*)take(f4);
+        w.rad = (float4*)take(f4);
+        w.hp = (float4*)take(f4);
+        w.rng = (uint4*)take(f4);
         w.sh_o = (float4*)take(f4);
         w.sh_d = (float4*)take(f4);
         w.sh_e = (float4*)take(f4);

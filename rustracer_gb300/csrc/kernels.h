@@ -38,17 +38,10 @@ struct WfState {
     float4* ray_d[2];   //   direction, path id | segment << kPidBits in .w
     float4* hit;        // t, u, v, instance id
     uint32_t* hit_prim;
-    // per path, one 64-byte record (two sectors, read and written whole by
-    // shade however scattered its path ids): throughput + Ray.t, radiance +
-    // volume_dis, hit point + RandomSeed, RNG counters (pixel stream, ray
-    // stream, ray-stream z)
-    float4* path;
-    __host__ __device__ __forceinline__ float4& tp(uint32_t p) const { return path[4 * (size_t)p]; }
-    __host__ __device__ __forceinline__ float4& rad(uint32_t p) const { return path[4 * (size_t)p + 1]; }
-    __host__ __device__ __forceinline__ float4& hp(uint32_t p) const { return path[4 * (size_t)p + 2]; }
-    __host__ __device__ __forceinline__ uint4& rng(uint32_t p) const {
-        return reinterpret_cast<uint4*>(path)[4 * (size_t)p + 3];
-    }
+    float4* tp;         // per path: throughput, Ray.t
+    float4* rad;        //   radiance, volume_dis
+    float4* hp;         //   hit point, RandomSeed
+    uint4* rng;         //   pixel-stream counter, ray-stream counter, ray-stream z
     float4* sh_o;       // shadow queue: origin, tmax
     float4* sh_d;       //   direction, path id
     float4* sh_e;       //   emission E, throughput.x

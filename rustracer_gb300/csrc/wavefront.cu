@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(256) wf_nrc_apply(WfState st, NrcWave nrc, uin
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 L = nrc.qout[i];
         const uint32_t pid = __float_as_uint(L.w) & kPidMask;
-        const float4 tp = st.tp(pid), r = st.rad(pid);
-        st.rad(pid) = f4(r.x + tp.x * fmaxf(L.x, 0.0f), r.y + tp.y * fmaxf(L.y, 0.0f), r.z + tp.z * fmaxf(L.z, 0.0f),
+        const float4 tp = st.tp[pid], r = st.rad[pid];
+        st.rad[pid] = f4(r.x + tp.x * fmaxf(L.x, 0.0f), r.y + tp.y * fmaxf(L.y, 0.0f), r.z + tp.z * fmaxf(L.z, 0.0f),
                          r.w);
     }
 }

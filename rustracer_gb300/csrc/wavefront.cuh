@@ -171,10 +171,10 @@ GB_D void camera_body(const Wv& w, const WfState& st, uint32_t pid) {
     camera_ray(J.ubo, x, y, W, J.out.height, rng, seed, o, d, tfar);
     st.ray_o[0][pid] = f4(o, 0.0f);
     st.ray_d[0][pid] = f4(d, __uint_as_float(pid | si << kPidBits));
-    st.tp(pid) = f4(1.0f, 1.0f, 1.0f, 0.0f);                   // throughput, Ray.t = 0
-    st.rad(pid) = f4(0.0f, 0.0f, 0.0f, -1.0f);                 // radiance, volume_dis = -1
-    st.hp(pid) = f4(0.0f, 0.0f, 0.0f, __uint_as_float(seed));  // hitPoint, RandomSeed
-    st.rng(pid) = make_uint4(rng.w, 0u, tea16(sample, 0x9E3779B9u), 0u);
+    st.tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);                   // throughput, Ray.t = 0
+    st.rad[pid] = f4(0.0f, 0.0f, 0.0f, -1.0f);                 // radiance, volume_dis = -1
+    st.hp[pid] = f4(0.0f, 0.0f, 0.0f, __uint_as_float(seed));  // hitPoint, RandomSeed
+    st.rng[pid] = make_uint4(rng.w, 0u, tea16(sample, 0x9E3779B9u), 0u);
 }
 
 // traceRayEXT for the extension queue of bounce b (closest hit).
@@ -275,8 +275,8 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             const PathXY P = decode_path(w, word, J.out.width);
             const uint32_t pid = P.pid;
             const float4 h4 = st.hit[R + q];
-            const float4 tp4 = st.tp(pid), rad4 = st.rad(pid), hp4 = st.hp(pid);
-            uint4 rg = st.rng(pid);
+            const float4 tp4 = st.tp[pid], rad4 = st.rad[pid], hp4 = st.hp[pid];
+            uint4 rg = st.rng[pid];
             Payload Rp;
             Rp.hitValue = Rp.scatterDir = Rp.emittance = f3(0.0f);
             Rp.needScatter = 0;
@@ -343,10 +343,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 tp *= Rp.hitValue;
                 if (!Rp.needScatter || Rp.t < 0.0f) cont = false;
             }
-            st.tp(pid) = f4(tp, Rp.t);
-            st.rad(pid) = f4(rad, Rp.volume_dis);
-            st.hp(pid) = f4(Rp.hitPoint, __uint_as_float(Rp.RandomSeed));
-            st.rng(pid) = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
+            st.tp[pid] = f4(tp, Rp.t);
+            st.rad[pid] = f4(rad, Rp.volume_dis);
+            st.hp[pid] = f4(Rp.hitPoint, __uint_as_float(Rp.RandomSeed));
+            st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
             }
@@ -404,9 +404,9 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
             const uint32_t pid = __float_as_uint(d4.w) & kPidMask;
             float3 e = f3(e4);
             if (!occluded) e += f3(c4);
-            const float4 r = st.rad(pid);
+            const float4 r = st.rad[pid];
             const float3 rad = f3(r) + f3(e4.w, c4.w, tpz) * e;
-            st.rad(pid) = f4(rad, r.w);
+            st.rad[pid] = f4(rad, r.w);
         });
     flush_trace_stats(ts, J.out.counters);
     if (blockIdx.x == w.blk0(2, jb) && threadIdx.x == 0)
@@ -426,7 +426,7 @@ GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave*
     float last_t = acc.w;
     for (uint32_t j = 0; j < sg.k; ++j) {
         const uint32_t pid = sg.path0 + li + j * sg.npw;
-        const float3 r = f3(st.rad(pid));
+        const float3 r = f3(st.rad[pid]);
         if (J.out.sample_radiance) {
             float* sr = J.out.sample_radiance + ((size_t)pix * J.ns + sg.si0 + j) * 3;
             sr[0] = r.x;
@@ -434,7 +434,7 @@ GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave*
             sr[2] = r.z;
         }
         sum += r;
-        last_t = st.tp(pid).w;
+        last_t = st.tp[pid].w;
         if constexpr (kNrc) {  // training sample: suffix radiance / throughput at the vertex
             const float4 sp = nrc->snap_pos[pid];
             if (sp.w != 0.0f) {
