@@ -213,3 +213,42 @@ def test_converged_vs_fp64_reference(gpu_ctx):
     relmse = float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
     assert np.isfinite(relmse) and relmse < 1e-2, relmse
     assert ref.mean() > 0.05  # the box is lit
+
+
+def _furnace(albedo):
+    """A closed 2x2x2 box, every wall emitting (1, 1, 1) with the reference's
+    'Lambertian' material of the given albedo, camera at the centre."""
+    from rustracer_gb300.scenes import GeoBuilder, lambert, _Soup
+    b = GeoBuilder()
+    m = b.add_material(lambert((albedo, albedo, albedo), emissive=(1.0, 1.0, 1.0)))
+    g = _Soup()
+    g.quad((-1, -1, 1), (1, -1, 1), (1, -1, -1), (-1, -1, -1))   # floor, normal +y
+    g.quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1))       # ceiling, -y
+    g.quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1))   # back, +z
+    g.quad((1, -1, 1), (-1, -1, 1), (-1, 1, 1), (1, 1, 1))       # front, -z
+    g.quad((-1, -1, 1), (-1, -1, -1), (-1, 1, -1), (-1, 1, 1))   # left, +x
+    g.quad((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1))       # right, -x
+    p, n, i = g.arrays()
+    b.add_mesh(p, i, m, n)
+    return b.finish(camera=dict(eye=(0.0, 0.0, 0.0), direction=(0.2, 0.1, -1.0), fov_deg=90.0),
+                    name=f"furnace{albedo}")
+
+
+def test_white_furnace(gpu_ctx):
+    """Analytic furnace (a closed box of unit emitters): every sample carries
+    the emission of its first hit at least once, so no radiance is below 1;
+    with albedo 0 only the dielectric specular lobe (Fresnel at normal
+    incidence 0.04) reflects, so the radiance stays below 1.1; with albedo
+    0.5 it grows (1 < mean < 1 / (1 - 0.75), the largest per-bounce weight of
+    the reference's lobes at roughness 1); the GPU meets the per-sample parity
+    contract against the oracle in both."""
+    import pyoracle as O
+    for albedo, lo, hi in ((0.0, 1.0, 1.1), (0.5, 1.05, 4.0)):
+        sd = _furnace(albedo)
+        ubo = sd.ubo(32, 32, samples=4, bounces=8, exposure=1.0)
+        ref = O.OracleScene(sd).render(ubo, 32, 32, want_samples=True)
+        r = render_gpu(gpu_ctx, sd, ubo, 32, 32)
+        s = r["samples"]
+        assert s.min() >= 1.0 and ref["samples"].min() >= 1.0
+        assert lo <= float(s.mean()) < hi, (albedo, float(s.mean()))
+        assert compare_samples(s, ref["samples"]) <= FLIP_MAX
