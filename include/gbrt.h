@@ -36,6 +36,7 @@ extern "C" {
 #define GBRT_E_NOT_BUILT     -5  /* render/trace before blas/tlas build */
 #define GBRT_E_NO_DEVICE     -6  /* no CUDA device, or the library was built without it */
 #define GBRT_E_BUSY          -7  /* job queue full / admission refused */
+#define GBRT_E_CANCELLED     -8  /* the job was cancelled (gbrt_job_cancel) */
 
 /* ------------------------------------------------------------------------ */
 /* Data contract: byte-for-byte mirrors of the reference's #[repr(C)] types  */
@@ -383,6 +384,12 @@ int gbrt_accum_create(gbrt_ctx* ctx, uint32_t width, uint32_t height, gbrt_accum
 int gbrt_accum_reset(gbrt_accum* acc);
 /* Copies width*height*4 floats (the running sum) to host memory. */
 int gbrt_accum_download(gbrt_accum* acc, float* rgba32f);
+/* Restores a running sum saved with gbrt_accum_download (width*height*4
+ * floats): with the saved sample count passed on as the next frame's
+ * ubo.total_number_of_samples - number_of_samples, progressive rendering
+ * resumes exactly where it stopped (checkpoint / resume of long renders; the
+ * reference resets its accumulation image instead, main.rs:336-353). */
+int gbrt_accum_upload(gbrt_accum* acc, const float* rgba32f);
 int gbrt_accum_destroy(gbrt_accum* acc);
 
 /* ------------------------------------------------------------------------ */
@@ -563,6 +570,18 @@ int gbrt_job_wait(gbrt_ctx* ctx, uint64_t job_id, uint32_t timeout_ms, gbrt_job_
 /* HBM budget for admitted jobs (0 = the device memory free when the first job
  * is submitted, minus 1 GiB) and the wave-filling policy. */
 int gbrt_jobs_configure(gbrt_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t policy);
+/* Cancels a job: a queued job ends at once, a running one once the waves
+ * already on the stream have drained (its image and accumulation are then
+ * partial); its status becomes GBRT_E_CANCELLED.  GBRT_E_INVALID for an
+ * unknown id, or when every path of the job is already on the stream (it then
+ * finishes normally). */
+int gbrt_job_cancel(gbrt_ctx* ctx, uint64_t job_id);
+/* Host-side fault injection for tests of the serving loop (no device fault
+ * is ever caused): GBRT_INJECT_ADMIT_OOM makes the next `count` job
+ * admissions fail as if the device allocation had run out of memory; the job
+ * ends with GBRT_E_OOM and the others carry on. */
+#define GBRT_INJECT_ADMIT_OOM 1u
+int gbrt_jobs_inject(gbrt_ctx* ctx, uint32_t kind, uint32_t count);
 
 /* ------------------------------------------------------------------------ */
 /* Neural radiance cache                                                     */

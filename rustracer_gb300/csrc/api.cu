@@ -724,6 +724,15 @@ int gbrt_accum_download(gbrt_accum* a, float* dst) {
     return GBRT_OK;
 }
 
+int gbrt_accum_upload(gbrt_accum* a, const float* src) {
+    if (!a || !src) return a ? fail(a->ctx, GBRT_E_INVALID, "src is NULL") : GBRT_E_INVALID;
+    if (a->jobs_pending.load()) return fail(a->ctx, GBRT_E_BUSY, "a job writes this accumulation buffer");
+    DeviceGuard g(a->ctx->device);
+    CU(a->ctx, cudaMemcpyAsync(a->buf.p, src, a->buf.bytes, cudaMemcpyHostToDevice, a->ctx->stream), "upload");
+    CU(a->ctx, cudaStreamSynchronize(a->ctx->stream), "sync");
+    return GBRT_OK;
+}
+
 int gbrt_accum_destroy(gbrt_accum* a) {
     if (!a) return GBRT_OK;
     if (a->jobs_pending.load()) return fail(a->ctx, GBRT_E_BUSY, "a job writes this accumulation buffer");

@@ -66,6 +66,7 @@ struct gbrt_ctx {
     std::mutex mu;
     gbrt_host::JobQueue* jobs = nullptr;  // created by the first gbrt_job_submit
     uint64_t jobs_budget = 0;             // gbrt_jobs_configure before the first job
+    std::atomic<uint32_t> inject_admit_oom{0};  // gbrt_jobs_inject: admissions still to fail
     uint32_t jobs_policy = 0;
 };
 

@@ -86,6 +86,7 @@ struct Job {
     std::vector<gbrt_skin_raw> skins;
     bool has_skins = false;
     gbrt_nrc* cache = nullptr;  // rendered alone through the cache (nrc_frame)
+    bool cancelled = false;
     gbrt_nrc_render_opts copts{};
     // progress
     uint32_t npix = 0, ns = 0, sbase = 0, chunk = 0;
@@ -105,6 +106,7 @@ struct Job {
 struct Wave {
     cudaEvent_t ev = nullptr;
     std::vector<Job*> finishing;  // jobs whose last segment this wave carried
+    bool cancel = false;          // a marker after a cancelled job's waves: it ends with GBRT_E_CANCELLED
 };
 
 }  // namespace
@@ -187,15 +189,20 @@ bool JobQueue::admit_one(std::unique_lock<std::mutex>& lk) {
     cudaStream_t st = ctx->stream;
     int rc = GBRT_OK;
     std::string msg;
-    cudaError_t e = j->frame_sum.alloc((size_t)j->npix * sizeof(float4), st);
+    cudaError_t e = cudaSuccess;
+    uint32_t inject = ctx->inject_admit_oom.load();
+    while (inject && !ctx->inject_admit_oom.compare_exchange_weak(inject, inject - 1)) {
+    }
+    if (inject) e = cudaErrorMemoryAllocation;  // injected (host side): as if the allocation had failed
+    if (e == cudaSuccess) e = j->frame_sum.alloc((size_t)j->npix * sizeof(float4), st);
     if (e == cudaSuccess && j->out_rgba8) e = j->img.alloc((size_t)j->npix * 4, st);
     if (e == cudaSuccess) e = j->counters.alloc(sizeof(DeviceCounters), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(j->frame_sum.p, 0, j->frame_sum.bytes, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(j->counters.p, 0, sizeof(DeviceCounters), st);
     if (e != cudaSuccess) {
-        cudaGetLastError();
+        if (!inject) cudaGetLastError();
         rc = e == cudaErrorMemoryAllocation ? GBRT_E_OOM : GBRT_E_CUDA;
-        msg = std::string("job admission: ") + cudaGetErrorString(e);
+        msg = std::string("job admission: ") + cudaGetErrorString(e) + (inject ? " (injected)" : "");
     } else if (j->has_skins) {
         rc = skin_scene(j->scene, j->skins.data(), (uint32_t)j->skins.size());
         if (rc != GBRT_OK) msg = ctx->err;
@@ -421,6 +428,15 @@ int JobQueue::launch_next(std::unique_lock<std::mutex>& lk) {
 
 // A wave's event has fired: finish the jobs it completed.  Lock held.
 void JobQueue::retire(Wave& w) {
+    if (w.cancel) {
+        for (Job* j : w.finishing) {
+            active.erase(std::find(active.begin(), active.end(), j));
+            finish_job(*this, j, GBRT_E_CANCELLED, "job cancelled");
+        }
+        free_events.push_back(w.ev);
+        cv_done.notify_all();
+        return;
+    }
     for (Job* j : w.finishing) {
         DeviceCounters dc{};
         cudaError_t e = cudaMemcpyAsync(&dc, j->counters.p, sizeof(dc), cudaMemcpyDeviceToHost, dl);
@@ -624,6 +640,58 @@ int gbrt_job_submit(gbrt_ctx* c, const gbrt_job_desc* d, uint64_t* job_id) {
         q->jobs.emplace(j->id, std::move(j));
     }
     q->cv_work.notify_all();
+    return GBRT_OK;
+}
+
+int gbrt_job_cancel(gbrt_ctx* c, uint64_t id) {
+    if (!c) return GBRT_E_INVALID;
+    if (!c->jobs) return fail(c, GBRT_E_INVALID, "unknown job id");
+    JobQueue* q = c->jobs;
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        auto it = q->jobs.find(id);
+        if (it == q->jobs.end()) return fail(c, GBRT_E_INVALID, "unknown job id");
+        Job* j = it->second.get();
+        if (j->state == GBRT_JOB_DONE) return fail(c, GBRT_E_INVALID, "the job has finished");
+        if (j->state == GBRT_JOB_QUEUED) {
+            q->queued.erase(std::find(q->queued.begin(), q->queued.end(), j));
+            finish_job(*q, j, GBRT_E_CANCELLED, "job cancelled");
+            q->cv_done.notify_all();
+            return GBRT_OK;
+        }
+        if (!j->paths_left || j->cancelled)
+            return fail(c, GBRT_E_INVALID, "every path of the job is already on the stream");
+        // running: no further segments; a marker after the waves already on the stream ends it
+        DeviceGuard g(c->device);
+        cudaEvent_t ev = nullptr;
+        if (!q->free_events.empty()) {
+            ev = q->free_events.back();
+            q->free_events.pop_back();
+        } else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, GBRT_E_CUDA, "event for the cancellation");
+        }
+        if (cudaEventRecord(ev, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            q->free_events.push_back(ev);
+            return fail(c, GBRT_E_CUDA, "event for the cancellation");
+        }
+        j->paths_left = 0;
+        j->cancelled = true;
+        Wave w;
+        w.ev = ev;
+        w.cancel = true;
+        w.finishing.push_back(j);
+        q->inflight.push_back(std::move(w));
+    }
+    q->cv_work.notify_all();
+    return GBRT_OK;
+}
+
+int gbrt_jobs_inject(gbrt_ctx* c, uint32_t kind, uint32_t count) {
+    if (!c) return GBRT_E_INVALID;
+    if (kind != GBRT_INJECT_ADMIT_OOM) return fail(c, GBRT_E_INVALID, "unknown injection");
+    c->inject_admit_oom.store(count);
     return GBRT_OK;
 }
 

@@ -23,6 +23,8 @@ from . import types as T
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libgbrt.so")
 
 OK, E_INVALID, E_CUDA, E_OOM, E_DEVICE_LIMIT, E_NOT_BUILT, E_NO_DEVICE, E_BUSY = 0, -1, -2, -3, -4, -5, -6, -7
+E_CANCELLED = -8
+INJECT_ADMIT_OOM = 1
 BUILD_NO_FLATTEN = 0x1
 BUILD_WIDTH4 = 0x2
 MODE_AUTO, MODE_MEGAKERNEL, MODE_WAVEFRONT = 0, 1, 2
@@ -49,6 +51,7 @@ SIGNATURES = {
     "gbrt_accum_create": (i32, [P, u32, u32, C.POINTER(P)]),
     "gbrt_accum_reset": (i32, [P]),
     "gbrt_accum_download": (i32, [P, P]),
+    "gbrt_accum_upload": (i32, [P, P]),
     "gbrt_accum_destroy": (i32, [P]),
     "gbrt_render": (i32, [P, P, P, P, P]),
     "gbrt_render_ex": (i32, [P, P, P, P, P, P]),
@@ -64,6 +67,8 @@ SIGNATURES = {
     "gbrt_job_submit": (i32, [P, P, C.POINTER(u64)]),
     "gbrt_job_poll": (i32, [P, u64, P]),
     "gbrt_job_wait": (i32, [P, u64, u32, P]),
+    "gbrt_job_cancel": (i32, [P, u64]),
+    "gbrt_jobs_inject": (i32, [P, u32, u32]),
     "gbrt_jobs_configure": (i32, [P, u64, u32]),
     "gbrt_nrc_create": (i32, [P, P, C.POINTER(P)]),
     "gbrt_nrc_destroy": (i32, [P]),
@@ -154,6 +159,10 @@ class Context:
     def jobs_configure(self, hbm_budget=0, policy=POLICY_SRPT):
         self.check(self.L.gbrt_jobs_configure(self.h, hbm_budget, policy))
 
+    def jobs_inject(self, kind, count):
+        """gbrt_jobs_inject: host-side fault injection (INJECT_ADMIT_OOM)."""
+        self.check(self.L.gbrt_jobs_inject(self.h, kind, count))
+
     def submit(self, scene, ubo, accum, image=True, skins=None, cache=None, min_roughness=0.0,
                train_samples=1 << 16, train_steps=1):
         """Queues one frame of `scene` into `accum` (through the radiance
@@ -199,6 +208,10 @@ class Job:
                      "stats": info["stats"].copy()}
         self.ctx.check(rc)
         return self.info
+
+    def cancel(self):
+        """gbrt_job_cancel."""
+        self.ctx.check(self.ctx.L.gbrt_job_cancel(self.ctx.h, self.id))
 
     def poll(self):
         if self.info is not None:
@@ -316,6 +329,11 @@ class Accum:
         out = np.zeros((self.h_, self.w, 4), np.float32)
         self.ctx.check(self.ctx.L.gbrt_accum_download(self.h, _p(out)))
         return out
+
+    def upload(self, rgba32f):
+        """gbrt_accum_upload: restore a running sum saved with download() (checkpoint / resume)."""
+        a = np.ascontiguousarray(rgba32f, np.float32).reshape(self.h_, self.w, 4)
+        self.ctx.check(self.ctx.L.gbrt_accum_upload(self.h, _p(a)))
 
     def close(self):
         if getattr(self, "h", None) and self.ctx.h:

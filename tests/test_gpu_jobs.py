@@ -192,3 +192,71 @@ def test_large_waves_equal_solo_render():
             assert np.array_equal(a.download(), acc_ref)
     finally:
         ctx.close()
+
+
+def test_job_cancel_queued_and_running():
+    """gbrt_job_cancel on a queued job (an HBM budget of one byte admits one
+    job at a time) ends it at once; on a running job whose segments are not
+    yet on the stream it ends after the waves in flight.  Both report
+    GBRT_E_CANCELLED, and the job left alone still equals its solo render."""
+    from rustracer_gb300 import build, gbrt
+    build.build()
+    ctx = gbrt.Context(0)
+    try:
+        sd = scenes.icosphere_scene(subdiv=3)
+        sc = gbrt.Scene(ctx, sd)
+        big = sd.ubo(1280, 720, samples=16, bounces=6, exposure=1.0)
+        img_ref, acc_ref = _solo(ctx, sc, big, 1280, 720)
+        # queued: one job admitted at a time
+        ctx.jobs_configure(hbm_budget=1, policy=gbrt.POLICY_FIFO)
+        acc_a, acc_b = gbrt.Accum(ctx, 1280, 720), gbrt.Accum(ctx, 64, 64)
+        ja = ctx.submit(sc, big, acc_a)
+        jb = ctx.submit(sc, sd.ubo(64, 64, samples=1, bounces=6, exposure=1.0), acc_b)
+        jb.cancel()
+        with pytest.raises(gbrt.GbrtError) as e:
+            jb.wait()
+        assert e.value.code == gbrt.E_CANCELLED
+        assert ja.wait()["status"] == 0
+        assert np.array_equal(ja.image.reshape(img_ref.shape), img_ref)
+        assert np.array_equal(acc_a.download(), acc_ref)
+        # running: first in submission order is the large job, so the second one's segments wait
+        ctx.jobs_configure(hbm_budget=1 << 34, policy=gbrt.POLICY_FIFO)
+        acc_c, acc_d = gbrt.Accum(ctx, 1280, 720), gbrt.Accum(ctx, 1280, 720)
+        jc = ctx.submit(sc, big, acc_c)
+        jd = ctx.submit(sc, big, acc_d)
+        jd.cancel()
+        with pytest.raises(gbrt.GbrtError) as e:
+            jd.wait()
+        assert e.value.code == gbrt.E_CANCELLED
+        assert jc.wait()["status"] == 0
+        assert np.array_equal(acc_c.download(), acc_ref)
+        with pytest.raises(gbrt.GbrtError):  # finished: nothing left to cancel
+            jc.cancel()
+    finally:
+        ctx.close()
+
+
+def test_injected_admission_failure():
+    """Host-side fault injection: the first admission fails as if out of
+    memory (GBRT_E_OOM); the other jobs of the batch still finish and equal
+    their solo renders."""
+    from rustracer_gb300 import build, gbrt
+    build.build()
+    ctx = gbrt.Context(0)
+    try:
+        sd = scenes.icosphere_scene(subdiv=2)
+        sc = gbrt.Scene(ctx, sd)
+        ubos = [sd.ubo(96, 64, samples=s, bounces=6, exposure=1.0) for s in (2, 3, 1)]
+        solo = [_solo(ctx, sc, u, 96, 64) for u in ubos]
+        ctx.jobs_inject(gbrt.INJECT_ADMIT_OOM, 1)
+        accs = [gbrt.Accum(ctx, 96, 64) for _ in ubos]
+        js = [ctx.submit(sc, u, a) for u, a in zip(ubos, accs)]
+        with pytest.raises(gbrt.GbrtError) as e:
+            js[0].wait()
+        assert e.value.code == gbrt.E_OOM
+        for j, a, (img, acc_ref) in list(zip(js, accs, solo))[1:]:
+            assert j.wait()["status"] == 0
+            assert np.array_equal(j.image.reshape(img.shape), img)
+            assert np.array_equal(a.download(), acc_ref)
+    finally:
+        ctx.close()
