@@ -261,6 +261,7 @@ def _linear_images(doc):
 
 
 def _textures(doc, bufs, base):
+    from .jpeg import read_jpeg
     from .png import read_png
     white = (1, 1, T.TEX_RGBA8_SRGB, T.WRAP_REPEAT, T.WRAP_REPEAT, np.full((1, 1, 4), 255, np.uint8))
     out = [white]
@@ -283,6 +284,8 @@ def _textures(doc, bufs, base):
                 data = open(os.path.join(base, im["uri"]), "rb").read()
             if data[:8] == b"\x89PNG\r\n\x1a\n":
                 img = read_png(data)
+            elif data[:2] == b"\xff\xd8":
+                img = read_jpeg(data)
         if img is None:
             out.append(white)
             continue
@@ -501,18 +504,23 @@ _FACE_ALIASES = {"posx": 0, "negx": 1, "posy": 2, "negy": 3, "posz": 4, "negz": 
 
 
 def load_cubemap(directory):
-    """Six square PNG faces named like the reference's skybox directories
-    (posx/negx/... or right/left/top/bottom/front/back, cubumap.rs Face) ->
-    (face size, RGBA8 bytes in +X, -X, +Y, -Y, +Z, -Z order) for
-    gbrt_skybox_set."""
+    """Six square PNG or JPEG faces named like the reference's skybox
+    directories (posx/negx/... or right/left/top/bottom/front/back, cubumap.rs
+    Face; the reference ships assets/skyboxs/Yokohama/*.jpg) -> (face size,
+    RGBA8 bytes in +X, -X, +Y, -Y, +Z, -Z order) for gbrt_skybox_set."""
+    from .jpeg import read_jpeg
     from .png import read_png
     faces = [None] * 6
     for name in os.listdir(directory):
         stem, ext = os.path.splitext(name)
-        if ext.lower() == ".png" and stem in _FACE_ALIASES:
+        if stem not in _FACE_ALIASES:
+            continue
+        if ext.lower() == ".png":
             faces[_FACE_ALIASES[stem]] = read_png(open(os.path.join(directory, name), "rb").read())
+        elif ext.lower() in (".jpg", ".jpeg"):
+            faces[_FACE_ALIASES[stem]] = read_jpeg(open(os.path.join(directory, name), "rb").read())
     if any(f is None for f in faces):
-        raise ValueError("a cubemap needs six PNG faces")
+        raise ValueError("a cubemap needs six PNG or JPEG faces")
     size = faces[0].shape[0]
     if any(f.shape[:2] != (size, size) for f in faces):
         raise ValueError("cubemap faces must be square and of one size")
