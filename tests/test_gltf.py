@@ -208,3 +208,42 @@ def test_cubemap_faces(tmp_path):
     size, data = gltf.load_cubemap(str(tmp_path))
     assert size == 4 and data.size == 6 * 4 * 4 * 4
     assert [int(data[k * 64]) for k in range(6)] == [0, 10, 20, 30, 40, 50]
+
+
+def test_generated_tangents():
+    """Tangents for normal-mapped primitives without a TANGENT attribute:
+    along +u of the texture mapping, orthogonal to the normal, unit length,
+    with the handedness of the v direction."""
+    from rustracer_gb300.gltf import generate_tangents
+    pos = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32)
+    nrm = np.tile([[0, 0, 1]], (4, 1)).astype(np.float32)
+    tri = np.array([[0, 1, 2], [0, 2, 3]])
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    t = generate_tangents(pos, nrm, uv, tri)
+    assert np.allclose(t, [[1, 0, 0, 1]] * 4, atol=1e-6)
+    t = generate_tangents(pos, nrm, uv[:, ::-1], tri)  # u along +y, v along +x: mirrored mapping
+    assert np.allclose(t[:, :3], [[0, 1, 0]] * 4, atol=1e-6) and np.all(t[:, 3] == -1)
+    # a sphere with longitude / latitude mapping: unit tangents orthogonal to the normals
+    from rustracer_gb300.scenes import _icosphere
+    v, f = _icosphere(2)
+    uvs = np.stack([np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi) + 0.5, np.arccos(np.clip(v[:, 1], -1, 1)) / np.pi], 1)
+    t = generate_tangents(v, v, uvs, f)
+    assert np.allclose(np.linalg.norm(t[:, :3], axis=1), 1.0, atol=1e-5)
+    assert np.abs(np.einsum("ij,ij->i", t[:, :3], v)).max() < 1e-4
+
+
+def test_loader_generates_tangents_for_normal_maps(tmp_path):
+    """A normal-mapped primitive with UVs and no TANGENT gets generated
+    tangents (geometry.rs:197-212); without the normal map it keeps the
+    default (1, 0, 0, 0)."""
+    tex = np.zeros((2, 2, 4), np.uint8)
+    png.write_png(str(tmp_path / "t.png"), tex)
+    path = tmp_path / "scene.gltf"
+    _write_gltf(str(path), (tmp_path / "t.png").read_bytes())
+    plain = gltf.load(str(path))
+    assert np.allclose(plain.vertices["tangent"][:4], [[1, 0, 0, 0]] * 4)
+    doc = json.load(open(path))
+    doc["materials"][0]["normalTexture"] = {"index": 0}
+    json.dump(doc, open(path, "w"))
+    mapped = gltf.load(str(path))
+    assert np.allclose(mapped.vertices["tangent"][:4], [[1, 0, 0, 1]] * 4, atol=1e-6)
