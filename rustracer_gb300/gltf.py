@@ -45,8 +45,9 @@ skin's joint matrices are world(joint) x inverse bind matrix, column-major,
 Normal-mapped primitives without tangents get generated ones
 (generate_tangents; the reference runs MikkTSpace there, geometry.rs:197-212);
 textures may be PNG or baseline JPEG (jpeg.py).  Morph targets are ignored,
-as in the reference (animation.rs:141-142).  Not reproduced: MikkTSpace's
-exact vertex splitting and degenerate rules, and glTF cameras.
+as in the reference (animation.rs:141-142), and so are glTF cameras (the
+reference's camera comes from its viewer).  Not reproduced: MikkTSpace's
+exact vertex splitting and degenerate rules.
 """
 import base64
 import json
