@@ -290,3 +290,30 @@ def test_float_skybox_equals_decoded_srgb():
             O.lib().orc_sample_skybox(o.h, d.ctypes.data_as(C.c_void_p), res[i].ctypes.data_as(C.c_void_p))
         out.append(res)
     assert np.allclose(out[0], out[1], rtol=2e-6, atol=1e-7)
+
+
+def test_float_skybox_bilinear_texels():
+    """HDR (RGBA32F) cube faces: a direction through a texel centre returns
+    that texel's value exactly, the face centre the mean of the four texels
+    of a 2x2 face (bilinear, clamp to edge inside the face; +Y face: s = x,
+    t = z)."""
+    import ctypes as C
+    import pyoracle as O
+    from rustracer_gb300 import scenes
+    faces = np.zeros((6, 2, 2, 4), np.float32)
+    faces[2, :, :, :3] = np.array([[[10.0, 1, 0], [20.0, 2, 0]], [[30.0, 3, 0], [40.0, 4, 0]]])  # [t][s]
+    faces[..., 3] = 1.0
+    sd = scenes.cornell()
+    sd.skybox = (2, faces.reshape(-1))
+    o = O.OracleScene(sd)
+
+    def sky(d):
+        d = np.array(d, np.float32)
+        out = np.zeros(3, np.float32)
+        O.lib().orc_sample_skybox(o.h, d.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p))
+        return out
+
+    assert np.array_equal(sky((-0.5, 1.0, -0.5)), np.float32([10, 1, 0]))
+    assert np.array_equal(sky((0.5, 1.0, -0.5)), np.float32([20, 2, 0]))
+    assert np.array_equal(sky((-0.5, 1.0, 0.5)), np.float32([30, 3, 0]))
+    assert np.allclose(sky((0.0, 1.0, 0.0)), [25.0, 2.5, 0.0], rtol=1e-6)
