@@ -348,9 +348,20 @@ int gbrt_blas_build(gbrt_scene* scene, const gbrt_geo_range* ranges, uint32_t n,
  * two-level through their geometry's BLAS. */
 int gbrt_tlas_build(gbrt_scene* scene, const gbrt_instance* instances, uint32_t n);
 
-/* Re-fits the TLAS for new instance transforms without a rebuild of the
- * BLASes.  The reference rebuilds the TLAS every animated frame
- * (crates/examples/gltf_viewer/src/main.rs:405-408). */
+/* New instance transforms for an animated frame.  Replaces the reference's
+ * per-frame create_top_as of animated scenes (crates/examples/gltf_viewer/
+ * src/main.rs:395-402, acceleration_structures.rs:136-172).  n must equal
+ * the built instance count.  When only the transforms changed (same
+ * geometries, masks, custom indices and flags, and, for instances kept under
+ * the TLAS, the same identity / non-identity class), the update is
+ * incremental: transformed instances merged into the world BVH re-transform
+ * their triangles, the binary world BVH is rebuilt with the fast Morton tree
+ * and the wide one refit in place (a full build once the refit's SAH cost
+ * proxy has drifted 1.3x); a TLAS is rebuilt over the instances' new world
+ * boxes with the BLASes untouched.  Any other change takes a full build, as
+ * gbrt_tlas_build.  Hits are the same as after gbrt_tlas_build with these
+ * instances.  GBRT_E_BUSY while the context has unfinished jobs.
+ * Synchronous. */
 int gbrt_tlas_update(gbrt_scene* scene, const gbrt_instance* instances, uint32_t n);
 
 /* Linear-blend skinning of every vertex with skin_index >= 0 (exactly
@@ -448,7 +459,14 @@ int gbrt_trace_rays_device(gbrt_scene* scene, const gbrt_ray* d_rays, uint32_t n
  *    that first call before any CUDA stream capture;
  *  - all calls on a device share the array: calls from one context are
  *    ordered by its stream, but calls that overlap on the GPU (two contexts
- *    or threads on the same device at once) race and corrupt each other.
+ *    or threads on the same device at once) race and corrupt each other;
+ *  - GBRT_E_BUSY while the context has unfinished jobs (they read the BVH);
+ *  - the binary world BVH is rebuilt; the wide (4- or 8-wide) copy keeps its
+ *    topology and is refit in place, so both traversal forms stay usable
+ *    (the refit tree loses quality as the mesh deforms; gbrt_tlas_build
+ *    builds a fresh one);
+ *  - a failure after the rebuild has started leaves the scene unbuilt:
+ *    later calls get GBRT_E_NOT_BUILT until gbrt_tlas_build.
  * Synchronous: returns after the rebuild has finished. */
 #define GBRT_NOALLOC_MAX_TRIANGLES 65536u
 int gbrt_scene_rebuild_noalloc(gbrt_scene* scene, const gbrt_vertex* d_vertices);
@@ -483,7 +501,7 @@ typedef struct gbrt_scene_info {
     uint32_t wide_width;       /* 4 or 8 */
     uint32_t refits;           /* refits since the last full build */
     uint32_t drift_rebuilds;   /* full rebuilds forced by refit drift */
-    uint32_t _pad;
+    uint32_t instance_updates; /* gbrt_tlas_update calls served incrementally (no full build) */
     double sah_built;          /* SAH cost proxy of the wide world BVH as built: summed child-box area
                                   over the root box's (0 when there is no wide world BVH) */
     double sah_now;            /* the same after the last refit */
@@ -592,7 +610,10 @@ int gbrt_jobs_inject(gbrt_ctx* ctx, uint32_t kind, uint32_t count);
  * features) and an MLP 32 -> 5 x 64 (ReLU) -> 3, trained online on path
  * suffixes.  Queries run the MLP on tensor cores in BF16 with FP32
  * accumulation: tcgen05.mma with the accumulator in tensor memory by
- * default, mma.sync with GBRT_NRC_QUERY_MMA_SYNC; training runs in FP32 with Adam (b1 0.9, b2 0.99, eps 1e-15)
+ * default, mma.sync with GBRT_NRC_QUERY_MMA_SYNC.  Training runs the
+ * forward and backward passes and the weight gradient on the tensor cores
+ * (mma.sync, BF16 operands, FP32 accumulation; GBRT_NRC_TRAIN_FP32: FP32 on
+ * the CUDA cores), then Adam (b1 0.9, b2 0.99, eps 1e-15) on FP32 masters
  * on the loss mean((y - t)^2 / (y^2 + 0.01)) (y not differentiated in the
  * denominator).  Positions are normalised to [box_lo, box_hi]. */
 typedef struct gbrt_nrc gbrt_nrc;
@@ -604,10 +625,11 @@ typedef struct gbrt_nrc_config {
     float learning_rate;       /* Adam step size (1e-2) */
     float box_lo[3], box_hi[3];
     uint64_t seed;             /* parameter initialisation */
-    uint32_t flags;            /* 0: queries on tcgen05; GBRT_NRC_QUERY_MMA_SYNC: on mma.sync */
+    uint32_t flags;            /* GBRT_NRC_* bits; 0: queries on tcgen05, training on mma.sync */
     uint32_t _pad;
 } gbrt_nrc_config;
-#define GBRT_NRC_QUERY_MMA_SYNC 0x1u
+#define GBRT_NRC_QUERY_MMA_SYNC 0x1u  /* queries on mma.sync instead of tcgen05 */
+#define GBRT_NRC_TRAIN_FP32     0x2u  /* training in FP32 on the CUDA cores instead of the tensor cores */
 
 int gbrt_nrc_create(gbrt_ctx* ctx, const gbrt_nrc_config* cfg, gbrt_nrc** out);
 int gbrt_nrc_destroy(gbrt_nrc* nrc);

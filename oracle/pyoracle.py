@@ -12,22 +12,25 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+DIAG_LIB_PATH = os.path.join(HERE, "_build", "liboracle_diag.so")
 
-_lib = None
+_libs = {}
 
 
 def build(force=False):
-    """Builds liboracle.so with the committed Makefile."""
-    if force or not os.path.exists(LIB_PATH):
+    """Builds liboracle.so and liboracle_diag.so with the committed Makefile."""
+    if force or not (os.path.exists(LIB_PATH) and os.path.exists(DIAG_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(diag=False):
+    """The oracle library: the plain build (timed CPU baseline), or with
+    diag=True the build with parity diagnostics (branch margins, ulp nudges),
+    which renders the same bits when no diagnostics are asked for."""
+    if diag not in _libs:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(DIAG_LIB_PATH if diag else LIB_PATH)
         P = C.c_void_p
         u32, i32 = C.c_uint32, C.c_int
         L.orc_scene_create.restype = P
@@ -43,6 +46,7 @@ def lib():
         L.orc_get_vertices.argtypes = [P, P, u32]
         L.orc_trace.argtypes = [P, P, u32, u32, P, i32, i32, P]
         L.orc_render.argtypes = [P, P, u32, u32, u32, u32, P, P, P, P, i32, i32, P]
+        L.orc_render_diag.argtypes = [P, P, u32, u32, u32, u32, P, P, P, P, P, u32, i32, i32, P]
         L.orc_pcg4d.argtypes = [P, P]
         L.orc_tea.restype = u32
         L.orc_tea.argtypes = [u32, u32]
@@ -57,8 +61,8 @@ def lib():
         L.orc_sample_skybox.argtypes = [P, P, P]
         L.orc_blend_hash.restype = u32
         L.orc_blend_hash.argtypes = [u32, u32, u32]
-        _lib = L
-    return _lib
+        _libs[diag] = L
+    return _libs[diag]
 
 
 STATS = np.dtype([("rays_camera", "<u8"), ("rays_extension", "<u8"), ("rays_shadow", "<u8"),
@@ -86,10 +90,11 @@ def tex_descs(textures):
 
 
 class OracleScene:
-    """The oracle's copy of a SceneData, with its BLAS/TLAS built."""
+    """The oracle's copy of a SceneData, with its BLAS/TLAS built.  diag=True
+    loads it into the diagnostics build (render(want_margins=..., nudge_ulps=...))."""
 
-    def __init__(self, sd, build_flags=0):
-        L = lib()
+    def __init__(self, sd, build_flags=0, diag=False):
+        L = self.L = lib(diag)
         self.sd = sd
         descs, keep = tex_descs(sd.textures)
         self.h = L.orc_scene_create(_p(sd.vertices), len(sd.vertices), _p(sd.indices), len(sd.indices),
@@ -110,16 +115,23 @@ class OracleScene:
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().orc_scene_destroy(self.h)
+            self.L.orc_scene_destroy(self.h)
             self.h = None
+
+    def tlas(self, instances):
+        """New instances (orc_tlas_build): the oracle builds its TLAS, and its
+        world BVH where instances are flattened, from scratch."""
+        instances = np.ascontiguousarray(instances)
+        assert self.L.orc_tlas_build(self.h, _p(instances), len(instances)) == 0
+        self._instances = instances
 
     def skin(self, skins):
         skins = np.ascontiguousarray(skins)
-        assert lib().orc_skin(self.h, _p(skins), len(skins)) == 0
+        assert self.L.orc_skin(self.h, _p(skins), len(skins)) == 0
 
     def vertices(self):
         out = np.zeros_like(self.sd.vertices)
-        assert lib().orc_get_vertices(self.h, _p(out), len(out)) == 0
+        assert self.L.orc_get_vertices(self.h, _p(out), len(out)) == 0
         return out
 
     def trace(self, rays, flags=0, fp64=False, threads=0):
@@ -127,23 +139,28 @@ class OracleScene:
         rays = np.ascontiguousarray(rays)
         hits = np.zeros(len(rays), T.HIT)
         st = np.zeros((), STATS)
-        assert lib().orc_trace(self.h, _p(rays), len(rays), flags, _p(hits), int(fp64), threads, _p(st)) == 0
+        assert self.L.orc_trace(self.h, _p(rays), len(rays), flags, _p(hits), int(fp64), threads, _p(st)) == 0
         return hits, st
 
     def render(self, ubo, width, height, rows=None, accum=None, want_samples=False, want_hits=False,
-               fp64=False, threads=0, out=True):
+               fp64=False, threads=0, out=True, want_margins=False, nudge_ulps=0):
+        """Renders rows [row0, row1) (all by default).  want_margins adds
+        'margins' [pixel][sample][2] (smallest branch-decision margin,
+        smallest secondary-hit barycentric); nudge_ulps > 0 moves every
+        transcendental by that many ulps (orc_render_diag)."""
         from rustracer_gb300 import types as T
         ns = int(ubo["number_of_samples"])
         row0, row1 = rows if rows is not None else (0, height)
         img = np.zeros((height, width, 4), np.uint8) if out else None
         samples = np.zeros((height * width, ns, 3), np.float32) if want_samples else None
         hits = np.zeros((height * width, ns), T.HIT) if want_hits else None
+        margins = np.full((height * width, ns, 2), np.inf, np.float32) if want_margins else None
         st = np.zeros((), STATS)
         ubo = np.ascontiguousarray(ubo)
-        rc = lib().orc_render(self.h, _p(ubo), width, height, row0, row1, _p(accum), _p(img), _p(samples),
-                              _p(hits), int(fp64), threads, _p(st))
+        rc = self.L.orc_render_diag(self.h, _p(ubo), width, height, row0, row1, _p(accum), _p(img), _p(samples),
+                                   _p(hits), _p(margins), int(nudge_ulps), int(fp64), threads, _p(st))
         assert rc == 0, rc
-        return dict(image=img, samples=samples, hits=hits, stats=st)
+        return dict(image=img, samples=samples, hits=hits, stats=st, margins=margins)
 
 
 # --- shader-library entry points ----------------------------------------

@@ -128,8 +128,28 @@ size_t texel_bytes(uint32_t format) {
     return format == GBRT_TEX_RGBA32F ? 16u : format == GBRT_TEX_RGBA16F ? 8u : 4u;
 }
 
+// kFeat* bits the materials use: the shade kernels compiled without a feature
+// serve scenes that never take its code.
+uint32_t material_features(const gbrt_material_raw* mats, uint32_t nmat) {
+    uint32_t f = 0;
+    for (uint32_t i = 0; i < nmat; ++i) {
+        const gbrt_material_raw& m = mats[i];
+        const gbrt_texture_info* tex[] = {&m.base_color_texture,     &m.metallic_roughness_texture,
+                                          &m.normal_texture,         &m.emissive_texture,
+                                          &m.transmission_texture,   &m.specular_texture,
+                                          &m.specular_color_texture, &m.sg_diffuse_texture,
+                                          &m.sg_specular_glossiness_texture};
+        for (const gbrt_texture_info* t : tex)
+            if (t->index >= 0) f |= gbrt::kFeatTextures;
+        if (m.workflow == 1u) f |= gbrt::kFeatSpecGloss;
+        if (m.unlit) f |= gbrt::kFeatDebug;
+    }
+    return f;
+}
+
 void refresh_view(gbrt_scene* s) {
     DevScene& v = s->view;
+    v.shade_feat = s->shade_feat;
     v.nodes = s->nodes.as<BNode2>();
     v.tris = s->tris.as<TriRec>();
     v.inst = s->inst.as<DevInstance>();
@@ -323,7 +343,8 @@ int build_all(gbrt_scene* s) {
             ihi[k] = bhi[d.blas_geo];
         }
         CU(c, upload(s->inst, hinst.data(), hinst.size(), st), "upload(instances)");
-        DevBuf d_ids, d_blo, d_bhi, d_lo, d_hi;
+        DevBuf &d_ids = s->tlas_ids_d, &d_blo = s->tlas_blo, &d_bhi = s->tlas_bhi, &d_lo = s->tlas_lo,
+               &d_hi = s->tlas_hi;
         CU(c, upload(d_ids, tlas_ids.data(), nt, st), "upload(tlas ids)");
         CU(c, upload(d_blo, ilo.data(), nt, st), "upload");
         CU(c, upload(d_bhi, ihi.data(), nt, st), "upload");
@@ -336,6 +357,8 @@ int build_all(gbrt_scene* s) {
         CU(c, build_instance_bvh(d_lo.as<float4>(), d_hi.as<float4>(), d_ids.as<uint32_t>(), nt,
                                  s->nodes.as<BNode2>(), tlas_node_base, s->tris.as<TriRec>(), tlas_tri_base, &r, st),
            "build TLAS");
+        s->tlas_node_base = tlas_node_base;
+        s->tlas_tri_base = tlas_tri_base;
         v.has_tlas = 1;
         v.tlas_root = r.root;
         v.tlas_lo = r.lo;
@@ -346,8 +369,65 @@ int build_all(gbrt_scene* s) {
         s->blas_cw_tris.release();
         CU(c, cudaStreamSynchronize(st), "sync after build");
     }
+    s->h_inst = std::move(hinst);
+    s->tlas_ids = std::move(tlas_ids);
+    s->flattened = false;
+    for (const DevInstance& d : s->h_inst) s->flattened = s->flattened || (flatten && !d.identity && (d.mask & 0xFFu));
     refresh_view(s);
     s->built = v.has_world || v.has_tlas;
+    return GBRT_OK;
+}
+
+// gbrt_tlas_update: the instances keep their geometries, masks and custom
+// indices and only their transforms move (the reference's animated frames,
+// gltf_viewer main.rs:395-402 -> create_top_as).  Transformed instances merged
+// into the world BVH re-transform their triangles: the binary world BVH is
+// rebuilt (Morton radix tree, one launch chain) and the wide one refit in
+// place, with the refit's drift check; a TLAS is rebuilt over the instances'
+// new world boxes, the BLASes untouched.  Anything else changing (a geometry,
+// a mask, an instance entering or leaving the world BVH) takes a full build.
+int update_instances(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
+    gbrt_ctx* c = s->ctx;
+    cudaStream_t st = c->stream;
+    bool same = s->h_inst.size() == n;
+    for (uint32_t i = 0; same && i < n; ++i) {
+        const gbrt_instance& a = s->instances[i];
+        const gbrt_instance& b = in[i];
+        const uint32_t mask = b.custom_index_and_mask >> 24;
+        same = a.custom_index_and_mask == b.custom_index_and_mask && a.blas_handle == b.blas_handle &&
+               a.sbt_offset_and_flags == b.sbt_offset_and_flags;
+        // without flattening, identity instances live in the world BVH and the others under the TLAS
+        if (same && !s->flattened && mask) same = (bool)s->h_inst[i].identity == is_identity(b.transform);
+    }
+    s->instances.assign(in, in + n);
+    if (!same) return build_all(s);
+    for (uint32_t i = 0; i < n; ++i) {
+        DevInstance& d = s->h_inst[i];
+        std::memcpy(d.xf, in[i].transform, sizeof(d.xf));
+        affine_inverse(d.xf, d.inv);
+        d.identity = is_identity(in[i].transform) && (d.mask & 0xFFu) != 0;
+    }
+    CU(c, cudaMemcpyAsync(s->inst.p, s->h_inst.data(), n * sizeof(DevInstance), cudaMemcpyHostToDevice, st),
+       "upload(instances)");
+    DevScene& v = s->view;
+    if (v.has_tlas) {
+        const uint32_t nt = (uint32_t)s->tlas_ids.size();
+        CU(c, instance_world_boxes(s->inst.as<DevInstance>(), s->tlas_ids_d.as<uint32_t>(), s->tlas_blo.as<float4>(),
+                                   s->tlas_bhi.as<float4>(), nt, s->tlas_lo.as<float4>(), s->tlas_hi.as<float4>(), st),
+           "instance boxes");
+        BvhResult r;
+        CU(c, build_instance_bvh(s->tlas_lo.as<float4>(), s->tlas_hi.as<float4>(), s->tlas_ids_d.as<uint32_t>(), nt,
+                                 s->nodes.as<BNode2>(), s->tlas_node_base, s->tris.as<TriRec>(), s->tlas_tri_base, &r,
+                                 st),
+           "rebuild TLAS");
+        v.tlas_root = r.root;
+        v.tlas_lo = r.lo;
+        v.tlas_hi = r.hi;
+    }
+    ++s->instance_updates;
+    if (s->flattened) return refit_world(s);
+    CU(c, cudaStreamSynchronize(st), "sync after instance update");
+    refresh_view(s);
     return GBRT_OK;
 }
 
@@ -559,6 +639,7 @@ int gbrt_scene_create(gbrt_ctx* c, const gbrt_vertex* v, uint32_t nv, const uint
     if ((e = upload(s->indices, idx, ni, st)) != cudaSuccess) return bail(e, "upload(indices)");
     if ((e = upload(s->prims, prims, ngeo, st)) != cudaSuccess) return bail(e, "upload(prims)");
     if ((e = upload(s->mats, mats, nmat, st)) != cudaSuccess) return bail(e, "upload(materials)");
+    s->shade_feat = material_features(mats, nmat);
     std::vector<DevTexture> dt(ntex);
     for (uint32_t i = 0; i < ntex; ++i) {
         const gbrt_texture_desc& t = tex[i];
@@ -634,8 +715,13 @@ int gbrt_tlas_build(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
 
 int gbrt_tlas_update(gbrt_scene* s, const gbrt_instance* in, uint32_t n) {
     if (!s) return GBRT_E_INVALID;
-    if (n != s->instances.size()) return fail(s->ctx, GBRT_E_INVALID, "instance count differs from the built TLAS");
-    return gbrt_tlas_build(s, in, n);
+    gbrt_ctx* c = s->ctx;
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
+    if (n && !in) return fail(c, GBRT_E_INVALID, "instances is NULL");
+    if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS with gbrt_tlas_build before updating it");
+    if (n != s->instances.size()) return fail(c, GBRT_E_INVALID, "instance count differs from the built TLAS");
+    DeviceGuard g(c->device);
+    return update_instances(s, in, n);
 }
 
 int gbrt_skin_and_refit(gbrt_scene* s, const gbrt_skin_raw* skins, uint32_t nskin) {
@@ -926,6 +1012,7 @@ int gbrt_scene_info_get(gbrt_scene* s, gbrt_scene_info* info) {
     info->wide_width = (uint32_t)cw_width(s);
     info->refits = s->refits;
     info->drift_rebuilds = s->rebuilds;
+    info->instance_updates = s->instance_updates;
     info->sah_built = s->cw_sah0;
     info->sah_now = s->cw_sah;
     return GBRT_OK;
@@ -1086,6 +1173,8 @@ int noalloc_setup(gbrt_ctx* c, void** out) {
 extern "C" int gbrt_scene_rebuild_noalloc(gbrt_scene* s, const gbrt_vertex* d_vertices) {
     if (!s) return GBRT_E_INVALID;
     gbrt_ctx* c = s->ctx;
+    // queued jobs read this scene's BVH and host view from the job thread
+    if (jobs_outstanding(c)) return fail(c, GBRT_E_BUSY, "jobs are running on this context");
     if (!s->built) return fail(c, GBRT_E_NOT_BUILT, "build the TLAS with gbrt_tlas_build before rebuilding");
     bool transformed = s->view.has_tlas;  // flattened transformed instances have no TLAS but count too
     for (const gbrt_instance& in : s->instances)
@@ -1103,23 +1192,44 @@ extern "C" int gbrt_scene_rebuild_noalloc(gbrt_scene* s, const gbrt_vertex* d_ve
     int rc = noalloc_setup(c, &base);
     if (rc != GBRT_OK) return rc;
     cudaStream_t st = c->stream;
-    if (d_vertices)
-        CU(c, cudaMemcpyAsync(s->vertices.p, d_vertices, s->vertices.bytes, cudaMemcpyDeviceToDevice, st),
-           "copy vertices");
+    // From here on the vertices and BVH pools are overwritten in place: after a
+    // failure they describe neither the old nor the new geometry, so the scene
+    // answers GBRT_E_NOT_BUILT until gbrt_tlas_build builds it again.
+    auto broken = [&](cudaError_t e, const char* what) {
+        s->built = false;
+        return cuda_fail(c, e, what);
+    };
+    cudaError_t e = cudaSuccess;
+    if (d_vertices &&
+        (e = cudaMemcpyAsync(s->vertices.p, d_vertices, s->vertices.bytes, cudaMemcpyDeviceToDevice, st)) !=
+            cudaSuccess)
+        return broken(e, "copy vertices");
     const BuildScratch scratch = bvh_scratch_carve(base, kNoallocMaxTriangles);
     BvhResult r;
-    CU(c, build_triangle_bvh_scratch(scratch, s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
-                                     s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)n,
-                                     s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st),
-       "allocation-free BVH rebuild");
-    CU(c, cudaStreamSynchronize(st), "sync after rebuild");
+    if ((e = build_triangle_bvh_scratch(scratch, s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                        s->prims.as<gbrt_priminfo>(), s->items.as<uint4>(), (uint32_t)n,
+                                        s->nodes.as<BNode2>(), 0, s->tris.as<TriRec>(), 0, &r, st)) != cudaSuccess)
+        return broken(e, "allocation-free BVH rebuild");
+    // The wide copy of the world BVH keeps its topology and is refit in place
+    // into the box buffer reserved at build time (kernels only, no allocation).
+    const bool wide = s->cw_count && s->cw_levels.size() >= 2 &&
+                      s->cw_boxes.bytes >= (size_t)s->cw_count * 2 * sizeof(float4) + 16;
+    double sah = 0.0;
+    if (wide && (e = refit_triangle_cwbvh(s->vertices.as<gbrt_vertex>(), s->indices.as<uint32_t>(),
+                                          s->prims.as<gbrt_priminfo>(), s->cw_nodes.as<CwNode>(),
+                                          s->cw_tris.as<TriRec>(), s->nworld, s->cw_levels, s->cw_boxes.as<float4>(),
+                                          st, s->inst.as<DevInstance>(), &sah)) != cudaSuccess)
+        return broken(e, "allocation-free refit of the wide BVH");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return broken(e, "sync after rebuild");
     s->view.world_root = r.root;
     s->view.world_lo = r.lo;
     s->view.world_hi = r.hi;
-    // the 8-wide copy of the world BVH now describes the old vertices: drop it
-    // so every traversal uses the rebuilt binary BVH
-    s->cw_count = 0;
-    s->view.cw_nodes = nullptr;
-    s->view.cw_tris = nullptr;
+    if (wide) {
+        ++s->refits;
+        s->cw_sah = sah;
+    } else {  // no wide copy to refit: traversal uses the rebuilt binary BVH
+        s->cw_count = 0;
+    }
+    refresh_view(s);
     return GBRT_OK;
 }

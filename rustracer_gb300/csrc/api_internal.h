@@ -83,6 +83,7 @@ struct gbrt_scene {
     uint32_t nd = 0, np = 0, sky_size = 0, sky_format = GBRT_TEX_RGBA8_SRGB;
     bool skinned = false;
     bool all_opaque = true;
+    uint32_t shade_feat = gbrt::kFeatAll;  // material features (kFeat* bits), set at creation
     // acceleration structures
     gbrt_host::DevBuf nodes, tris, inst, items;
     gbrt_host::DevBuf cw_nodes, cw_tris;  // 8-wide world BVH used by the wavefront traversal
@@ -94,6 +95,15 @@ struct gbrt_scene {
     double cw_sah0 = 0.0;              // SAH cost proxy of the 8-wide world BVH as built (refit drift reference)
     double cw_sah = 0.0;               // ... after the last refit
     uint32_t refits = 0, rebuilds = 0; // refits since the build; full rebuilds forced by refit drift
+    // kept by the build for gbrt_tlas_update (transforms only): the device
+    // instances as uploaded, the TLAS's instances and BLAS root boxes, and
+    // where the TLAS sits in the pools
+    std::vector<gbrt::DevInstance> h_inst;
+    std::vector<uint32_t> tlas_ids;
+    gbrt_host::DevBuf tlas_ids_d, tlas_blo, tlas_bhi, tlas_lo, tlas_hi;
+    uint32_t tlas_node_base = 0, tlas_tri_base = 0;
+    bool flattened = false;            // transformed instances were merged into the world BVH
+    uint32_t instance_updates = 0;     // gbrt_tlas_update calls served incrementally
     uint32_t cw_count = 0;
     bool built = false;
     std::atomic<uint32_t> jobs_pending{0};  // submitted, unfinished jobs that render this scene

@@ -83,10 +83,13 @@ GB_D bool sample_light_ris(const DevScene& s, uint4& rng, float3 P, float3 Ng, g
 // RayTracing.rchit:136-477 for the hit h of a ray with world direction wdir.
 // shadow(origin, dir, tmax, C) handles the NEE shadow ray: it must add C to
 // R.emittance when the light is unoccluded (the megakernel traces it at once,
-// the wavefront defers it to the any-hit kernel).
-template <class ShadowFn>
+// the wavefront defers it to the any-hit kernel).  kFeat (kFeat* bits) lists
+// the material features compiled in; the caller picks a form that covers the
+// scene's DevScene::shade_feat and the frame's debug settings.
+template <uint32_t kFeat = kFeatAll, class ShadowFn>
 GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const Hit& h, float3 wdir, PathStats& ps,
                       ShadowFn&& shadow) {
+    constexpr bool kTex = (kFeat & kFeatTextures) != 0;
     ps.shaded++;
     const DevInstance& in = s.inst[h.inst];
     const uint32_t custom = in.custom;
@@ -122,12 +125,12 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     float3 origin = point_xform(T, pos);
 
     float4 color4 = col * f4(mat.base_color[0], mat.base_color[1], mat.base_color[2], mat.base_color[3]);
-    if (mat.base_color_texture.index >= 0)
+    if (kTex && mat.base_color_texture.index >= 0)
         color4 = color4 * texture(s, mat.base_color_texture.index, get_uv(uv01, mat.base_color_texture.coord));
     float3 color = f3(color4);
     R.needScatter = 0;
     R.hitPoint = pos;
-    if (mat.normal_texture.index >= 0) {  // getNormal, rchit:124-129,180-185
+    if (kTex && mat.normal_texture.index >= 0) {  // getNormal, rchit:124-129,180-185
         const float4 tn = texture(s, mat.normal_texture.index, get_uv(uv01, mat.normal_texture.coord));
         const float3 nt = normalize3(f3(tn) * 2.0f - 1.0f);
         const float3 tm = f3(tangent);
@@ -143,23 +146,23 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     const float3 N = dot(Ng, normal) < 0.0f ? -normal : normal;  // outwardNormal
 
     float3 emittance = f3(mat.emissive_factor[0], mat.emissive_factor[1], mat.emissive_factor[2]);
-    if (mat.emissive_texture.index >= 0)
+    if (kTex && mat.emissive_texture.index >= 0)
         emittance *= f3(texture(s, mat.emissive_texture.index, get_uv(uv01, mat.emissive_texture.coord)));
     float metallic = mat.metallic_factor, roughness = mat.roughness_factor;
-    if (mat.metallic_roughness_texture.index >= 0) {
+    if (kTex && mat.metallic_roughness_texture.index >= 0) {
         const float4 mr = texture(s, mat.metallic_roughness_texture.index,
                                   get_uv(uv01, mat.metallic_roughness_texture.coord));
         roughness *= mr.y;
         metallic *= mr.z;
     }
     float3 spec_wf = f3(1.0f);
-    const bool sg = mat.workflow == 1u;
+    const bool sg = (kFeat & kFeatSpecGloss) && mat.workflow == 1u;
     if (sg) {  // rchit:216-239
         float4 df = ldg4(mat.sg_diffuse_factor);
         float4 sgf = ldg4(mat.sg_specular_glossiness_factor);
-        if (mat.sg_diffuse_texture.index >= 0)
+        if (kTex && mat.sg_diffuse_texture.index >= 0)
             df = df * texture(s, mat.sg_diffuse_texture.index, get_uv(uv01, mat.sg_diffuse_texture.coord));
-        if (mat.sg_specular_glossiness_texture.index >= 0)
+        if (kTex && mat.sg_specular_glossiness_texture.index >= 0)
             sgf = sgf * texture(s, mat.sg_specular_glossiness_texture.index,
                                 get_uv(uv01, mat.sg_specular_glossiness_texture.coord));
         spec_wf = f3(sgf);
@@ -171,11 +174,11 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     float transmission = 0.0f;
     if (mat.transmission_exist) {
         transmission = mat.transmission_factor;
-        if (mat.transmission_texture.index >= 0)
+        if (kTex && mat.transmission_texture.index >= 0)
             transmission *= texture(s, mat.transmission_texture.index, get_uv(uv01, mat.transmission_texture.coord)).x;
     }
-    uint32_t mapping = ubo.mapping;
-    if (mat.unlit) mapping = 5u;  // ALBEDO
+    uint32_t mapping = (kFeat & kFeatDebug) ? ubo.mapping : 0u;
+    if ((kFeat & kFeatDebug) && mat.unlit) mapping = 5u;  // ALBEDO
     switch (mapping) {  // rchit:258-286
         case 5: R.emittance = color; return;
         case 3: R.emittance = f3(1.0f - h.u - h.v, h.u, h.v); return;
@@ -190,9 +193,9 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     }
     float spec_factor = mat.specular_factor;
     float3 spec_color = f3(mat.specular_color_factor[0], mat.specular_color_factor[1], mat.specular_color_factor[2]);
-    if (mat.specular_texture.index >= 0)
+    if (kTex && mat.specular_texture.index >= 0)
         spec_factor *= texture(s, mat.specular_texture.index, get_uv(uv01, mat.specular_texture.coord)).w;
-    if (mat.specular_color_texture.index >= 0)
+    if (kTex && mat.specular_color_texture.index >= 0)
         spec_color *= f3(texture(s, mat.specular_color_texture.index, get_uv(uv01, mat.specular_color_texture.coord)));
 
     R.hitPoint = origin;
@@ -263,7 +266,7 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     R.hitPoint = origin;
     R.scatterDir = dir;
     R.hitValue = throughput;
-    if (ubo.debug == 1u) {  // rchit:437-474 (legacy branch, D5)
+    if ((kFeat & kFeatDebug) && ubo.debug == 1u) {  // rchit:437-474 (legacy branch, D5)
         if (m.transmission > 0.0f) {
             const float eta = frontFace ? 1.0f / mat.ior : mat.ior;
             const float3 refr = refract3(wdir, N, eta);

@@ -108,6 +108,15 @@ struct DevScene {
     uint32_t all_opaque; // every geometry is OPAQUE: the any-hit test never runs
     uint32_t prefer_binary;  // autotuner's choice: traverse the binary layout even where 8-wide nodes exist
     uint32_t sort_rays;      // autotuner's choice: shade writes each block's extension rays grouped by octant
+    uint32_t shade_feat;     // kFeat* bits the scene's materials use (shade kernels specialise on them)
 };
+
+// Material features of the hit group (closest_hit) a shade kernel may be
+// compiled without.  A scene whose materials never use a feature never takes
+// its code, so a kernel compiled without it returns the same bits.
+constexpr uint32_t kFeatTextures = 1u;   // some material samples a texture
+constexpr uint32_t kFeatSpecGloss = 2u;  // some material uses the specular-glossiness workflow
+constexpr uint32_t kFeatDebug = 4u;      // unlit materials, a debug mapping or the legacy debug branch
+constexpr uint32_t kFeatAll = 7u;
 
 }  // namespace gbrt

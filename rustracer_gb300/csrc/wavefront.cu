@@ -42,8 +42,13 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
     wf_extend(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     extend_body<kMode>(w, st, b, 0u);
 }
-__global__ void __launch_bounds__(kShadeThreads, kShadeMinBlocks) wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
-    shade_body(w, st, b);
+// kFeat: the material features compiled in (kFeatAll, or 0 for scenes
+// without textures, specular-glossiness or debug shading, whose smaller body
+// runs at more resident blocks).
+template <uint32_t kFeat>
+__global__ void __launch_bounds__(kShadeThreads, kFeat ? kShadeMinBlocks : kShadePlainMinBlocks)
+    wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
+    shade_body<SingleWave, false, kFeat>(w, st, b);
 }
 template <int kMode>
 __global__ void __launch_bounds__(128, trace_minb(kMode))
@@ -97,7 +102,7 @@ cudaError_t init_wavefront_constants(const float* srgb_lut) {
 namespace {
 struct Grid {
     int dev = -1;
-    int extend = 0, shade = 0, shadow = 0;
+    int extend = 0, shade = 0, shade_plain = 0, shadow = 0;
 };
 Grid g_grid;
 
@@ -109,7 +114,12 @@ cudaError_t grids(Grid& g) {
     int sms = 0, be = 0, bs = 0, bh = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, wf_extend<kTraceWide>, 128, 0)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade, kShadeThreads, 0)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade<kFeatAll>, kShadeThreads, 0)) != cudaSuccess)
+        return e;
+    int bp = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp, wf_shade<0u>, kShadeThreads, 0)) != cudaSuccess)
+        return e;
+    g.shade_plain = sms * (bp > 0 ? bp : 1);
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
     g.extend = sms * (be > 0 ? be : 1);
     g.shade = sms * (bs > 0 ? bs : 1);
@@ -204,6 +214,8 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
     J.tfar = ubo.orthographic_fov_dis > 0.0f ? 100000.0f : 10000.0f;
     J.path0 = 0;
     const int mode = trace_mode(s);
+    // the shade form: the scene's material features and this frame's debug settings
+    const uint32_t feat = s.shade_feat | (ubo.mapping != 0u || ubo.debug == 1u ? kFeatDebug : 0u);
     // waves: k samples of a pixel range, k * npw <= cap
     for (uint32_t px0 = 0; px0 < npix;) {
         const uint32_t npw = npix - px0 < cap ? npix - px0 : cap;
@@ -231,7 +243,8 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 if (side && b > 0 && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
                 tb(1);
                 if (nrc) wf_shade_nrc<<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b, *nrc);
-                else wf_shade<<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b);
+                else if (feat == 0u) wf_shade<0u><<<g_grid.shade_plain, kShadeThreads, 0, stream>>>(w, st, b);
+                else wf_shade<kFeatAll><<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b);
                 te();
                 if (nrc && b >= 1 && !nrc->disabled) {  // cache queries of the paths that stopped here
                     tb(3);

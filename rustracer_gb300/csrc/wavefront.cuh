@@ -48,8 +48,13 @@ namespace gbrt {
 #ifndef GBRT_SHADE_MINB
 #define GBRT_SHADE_MINB 2
 #endif
+#ifndef GBRT_SHADE_PLAIN_MINB
+#define GBRT_SHADE_PLAIN_MINB 3
+#endif
 constexpr int kShadeThreads = GBRT_SHADE_THREADS;  // block size of the shade kernels
 constexpr int kShadeMinBlocks = GBRT_SHADE_MINB;   // resident blocks per SM the shade kernels are compiled for
+// ... and the form without textures, specular-glossiness and debug shading
+constexpr int kShadePlainMinBlocks = GBRT_SHADE_PLAIN_MINB;
 
 GB_D uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -237,7 +242,7 @@ GB_D uint32_t nrc_train_hash(uint32_t pix, uint32_t sample) {
     return h & 0xFFFFu;
 }
 
-template <class Wv, bool kNrc = false>
+template <class Wv, bool kNrc = false, uint32_t kFeat = kFeatAll>
 GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* nrc = nullptr) {
     const uint32_t jb = w.block_job(1);
     const WaveJob& J = w.job(jb);
@@ -315,7 +320,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 h.inst = inst;
                 h.prim = st.hit_prim[R + q];
                 h.bgeo = 0;
-                closest_hit(s, ubo, Rp, h, d, ps, [&](float3 o_, float3 d_, float t_, float3 C) {
+                closest_hit<kFeat>(s, ubo, Rp, h, d, ps, [&](float3 o_, float3 d_, float t_, float3 C) {
                     shadow = true;
                     so = o_;
                     sd = d_;

@@ -233,6 +233,7 @@ class NrcConfig(C.Structure):
 
 
 NRC_QUERY_MMA_SYNC = 0x1
+NRC_TRAIN_FP32 = 0x2
 
 
 class NrcRenderOpts(C.Structure):
@@ -421,12 +422,14 @@ class Scene:
                     ms_sorted=float(rep[3]), chosen_width=int(u[0]), sort_rays=int(u[1]))
 
     def info(self):
-        """gbrt_scene_info_get: world BVH sizes, refit count, drift rebuilds and SAH cost proxies."""
+        """gbrt_scene_info_get: world BVH sizes, refit count, drift rebuilds, incremental instance
+        updates and SAH cost proxies."""
         raw = np.zeros(5, np.float64)
         self.ctx.check(self.ctx.L.gbrt_scene_info_get(self.h, _p(raw)))
         u = raw[:3].view(np.uint32)
         return dict(world_triangles=int(u[0]), wide_nodes=int(u[1]), wide_width=int(u[2]), refits=int(u[3]),
-                    drift_rebuilds=int(u[4]), sah_built=float(raw[3]), sah_now=float(raw[4]))
+                    drift_rebuilds=int(u[4]), instance_updates=int(u[5]), sah_built=float(raw[3]),
+                    sah_now=float(raw[4]))
 
     def set_tuning(self, width=8, sort_rays=False):
         """gbrt_scene_set_tuning: BVH width 2/4/8 and the ray-sort key, set directly."""
