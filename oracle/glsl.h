@@ -19,6 +19,16 @@
 
 namespace glsl {
 
+// Parity diagnostics (the ORC_DIAG build of the oracle only): every dot
+// product and normalised vector passes through diag_round, which moves it by
+// a few ulps in nudge mode -- the size of the differences that fused
+// multiply-adds make on the GPU.  Without ORC_DIAG it is the identity.
+#ifdef ORC_DIAG
+float diag_round(float r);
+#else
+inline float diag_round(float r) { return r; }
+#endif
+
 struct vec2 {
     float x, y;
     vec2() : x(0), y(0) {}
@@ -86,13 +96,16 @@ inline vec3& operator*=(vec3& a, float s) { a = a * s; return a; }
 inline vec3& operator/=(vec3& a, float s) { a = a / s; return a; }
 inline bool operator==(vec3 a, vec3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 inline bool operator!=(vec3 a, vec3 b) { return !(a == b); }
-inline float dot(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline float dot(vec3 a, vec3 b) { return diag_round(a.x * b.x + a.y * b.y + a.z * b.z); }
 inline vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
 inline float length(vec3 a) { return std::sqrt(dot(a, a)); }
-inline vec3 normalize(vec3 a) { return a * inversesqrt(dot(a, a)); }
+inline vec3 normalize(vec3 a) {
+    const vec3 r = a * inversesqrt(dot(a, a));
+    return vec3(diag_round(r.x), diag_round(r.y), diag_round(r.z));
+}
 inline vec3 min(vec3 a, vec3 b) { return vec3(std::min(a.x, b.x), std::min(a.y, b.y), std::min(a.z, b.z)); }
 inline vec3 max(vec3 a, vec3 b) { return vec3(std::max(a.x, b.x), std::max(a.y, b.y), std::max(a.z, b.z)); }
 inline vec3 mix(vec3 x, vec3 y, float a) { return x * (1.0f - a) + y * a; }

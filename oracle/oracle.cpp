@@ -46,6 +46,74 @@ using namespace glsl;
 namespace {
 
 // ---------------------------------------------------------------------------
+// Parity diagnostics (not shader semantics), compiled into the ORC_DIAG build
+// (liboracle_diag.so) that the tests use; the timed CPU baseline
+// (liboracle.so) carries none of it.
+//
+// A GPU sample can leave the 1e-4 band around the oracle's sample when its
+// path meets a decision whose operands sit so close to the threshold that
+// ulp-level differences in the arithmetic before it (CUDA's sin/cos/pow/exp/
+// log against libm's, fused multiply-adds) take the other side, or when the
+// path amplifies those ulps continuously (a GGX lobe evaluated near its peak
+// cancels 1 - NdotH^2).  Per sample the oracle records:
+//  - margin[0]: the smallest |operand - threshold| of the decisions taken:
+//    Russian roulette (rgen:108-118), BRDF lobe choice (rchit:357-366), RIS
+//    acceptance (rchit:109), the light's back-face skip (rchit:98), front-face
+//    and outward-normal sides (rchit:189-193), TIR (PBR.glsl:689-692), the
+//    facing tests of the indirect sample (PBR.glsl:656) and of the NEE BRDF
+//    (PBR.glsl:539-540,737), the rotation's pole case (PBR.glsl:365),
+//    MASK/BLEND opacity tests of secondary rays (rahit:98,102), the
+//    directional light's side in the miss shader (rmiss:22) and the sky's
+//    cube-face choice;
+//  - margin[1]: the smallest barycentric coordinate of any secondary hit
+//    (distance to the triangle's nearest edge, where a ray nudged by an ulp
+//    can hit the neighbour or miss).
+// Every operand here is a uniform random number, a probability, a cosine or
+// a barycentric, all of unit scale, so the margins are absolute.  Decisions
+// between integer-exact quantities (the uniform light pick) come out the same
+// on both sides and are not logged.  In nudge mode every transcendental
+// result, dot product and normalised vector component is moved by +-k ulps
+// (sign drawn from a per-sample counter hash): samples that then leave the
+// 1e-4 band are ill-conditioned at the ulp level.
+// ---------------------------------------------------------------------------
+struct SampleDiag {
+    float margin[2];
+    uint32_t nudge_ulps;
+    uint32_t nudge_state;
+};
+#ifdef ORC_DIAG
+thread_local SampleDiag* g_diag = nullptr;
+inline void note_margin(float m) {
+    if (g_diag) g_diag->margin[0] = std::min(g_diag->margin[0], std::fabs(m));
+}
+inline void note_edge(float m) {
+    if (g_diag) g_diag->margin[1] = std::min(g_diag->margin[1], std::fabs(m));
+}
+inline float nudged(float r) {
+    if (!g_diag || !g_diag->nudge_ulps || !std::isfinite(r)) return r;
+    uint32_t h = g_diag->nudge_state = g_diag->nudge_state * 747796405u + 2891336453u;
+    h = ((h >> ((h >> 28u) + 4u)) ^ h) * 277803737u;
+    const float to = (h >> 31) ? INFINITY : -INFINITY;
+    for (uint32_t k = 0; k < g_diag->nudge_ulps; ++k) r = std::nextafter(r, to);
+    return r;
+}
+#else
+constexpr SampleDiag* g_diag = nullptr;
+inline void note_margin(float) {}
+inline void note_edge(float) {}
+inline float nudged(float r) { return r; }
+#endif
+// The shaders' transcendentals, nudged in diagnostics mode.
+inline float t_pow(float a, float b) { return nudged(std::pow(a, b)); }
+inline float t_sin(float a) { return nudged(std::sin(a)); }
+inline float t_cos(float a) { return nudged(std::cos(a)); }
+inline vec3 t_exp(vec3 a) { return vec3(nudged(std::exp(a.x)), nudged(std::exp(a.y)), nudged(std::exp(a.z))); }
+inline vec3 t_log(vec3 a) { return vec3(nudged(std::log(a.x)), nudged(std::log(a.y)), nudged(std::log(a.z))); }
+// Seed of a sample's nudge signs (mixed with the nudge size, so each size
+// draws other signs).
+inline uint32_t nudge_seed(uint32_t x, uint32_t y, uint32_t s) { return (x * 73856093u) ^ (y * 19349663u) ^ (s * 83492791u) ^ 0x5bd1e995u; }
+
+// ---------------------------------------------------------------------------
 // lib/Random.glsl
 // ---------------------------------------------------------------------------
 // InitRandomSeed, Random.glsl:12-25 (TEA, 16 rounds).
@@ -166,7 +234,7 @@ struct MaterialBrdf {
 float Schlick(const float cosine, const float refractionIndex) {  // PBR.glsl:48-53
     float r0 = (1.0f - refractionIndex) / (1.0f + refractionIndex);
     r0 *= r0;
-    return r0 + (1.0f - r0) * std::pow(1.0f - cosine, 5.0f);
+    return r0 + (1.0f - r0) * t_pow(1.0f - cosine, 5.0f);
 }
 
 void matBuild(MaterialBrdf& m) {  // PBR.glsl:195-206
@@ -182,7 +250,7 @@ float saturate(float x) { return clamp(x, 0.0f, 1.0f); }  // PBR.glsl:212
 float luminance(vec3 rgb) { return dot(rgb, vec3(0.2126f, 0.7152f, 0.0722f)); }  // :221-224
 
 vec3 evalFresnel(vec3 f0, float f90, float NdotS) {  // PBR.glsl:228-243
-    return f0 + (f90 - f0) * std::pow(1.0f - NdotS, 5.0f);
+    return f0 + (f90 - f0) * t_pow(1.0f - NdotS, 5.0f);
 }
 
 float Smith_G_a(float alpha, float NdotS) {  // PBR.glsl:248-250
@@ -230,6 +298,7 @@ BRDFProb getBrdfProbability(const MaterialBrdf& mat, vec3 V, vec3 shadingNormal)
 }
 
 vec4 getRotationToZAxis(vec3 v) {  // PBR.glsl:362-368
+    note_margin(v.z + 0.99999f);
     if (v.z < -0.99999f) return vec4(1.0f, 0.0f, 0.0f, 0.0f);
     return normalize(vec4(v.y, -v.x, 0.0f, 1.0f + v.z));
 }
@@ -243,7 +312,7 @@ vec4 invertRotation(vec4 q) { return vec4(-q.x, -q.y, -q.z, q.w); }  // PBR.glsl
 vec3 sampleHemisphere(vec2 u) {  // PBR.glsl:381-394
     float a = std::sqrt(u.x);
     float b = TWO_PI * u.y;
-    return vec3(a * std::cos(b), a * std::sin(b), std::sqrt(1.0f - u.x));
+    return vec3(a * t_cos(b), a * t_sin(b), std::sqrt(1.0f - u.x));
 }
 
 vec3 sampleGGXVNDF(vec3 Ve, vec2 alpha2D, vec2 u) {  // PBR.glsl:413-436
@@ -253,8 +322,8 @@ vec3 sampleGGXVNDF(vec3 Ve, vec2 alpha2D, vec2 u) {  // PBR.glsl:413-436
     vec3 T2 = cross(Vh, T1);
     float r = std::sqrt(u.x);
     float phi = TWO_PI * u.y;
-    float t1 = r * std::cos(phi);
-    float t2 = r * std::sin(phi);
+    float t1 = r * t_cos(phi);
+    float t2 = r * t_sin(phi);
     float s = 0.5f * (1.0f + Vh.z);
     t2 = mix(std::sqrt(1.0f - t1 * t1), t2, s);
     vec3 Nh = t1 * T1 + t2 * T2 + std::sqrt(std::max(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;
@@ -275,8 +344,8 @@ float frostbiteDisneyDiffuse(const BrdfData& d) {  // PBR.glsl:486-496
     float energyBias = 0.5f * d.roughness;
     float energyFactor = mix(1.0f, 1.0f / 1.51f, d.roughness);
     float FD90MinusOne = energyBias + 2.0f * d.LdotH * d.LdotH * d.roughness - 1.0f;
-    float FDL = 1.0f + (FD90MinusOne * std::pow(1.0f - d.NdotL, 5.0f));
-    float FDV = 1.0f + (FD90MinusOne * std::pow(1.0f - d.NdotV, 5.0f));
+    float FDL = 1.0f + (FD90MinusOne * t_pow(1.0f - d.NdotL, 5.0f));
+    float FDV = 1.0f + (FD90MinusOne * t_pow(1.0f - d.NdotV, 5.0f));
     return FDL * FDV * energyFactor;
 }
 vec3 evalFrostbiteDisneyDiffuse(const BrdfData& d) {  // PBR.glsl:516-518
@@ -331,6 +400,7 @@ vec3 sampleSpecularMicrofacet(vec3 Vlocal, float alpha, float alphaSquared, vec3
 bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, vec3 V,
                               const MaterialBrdf& material, const uint32_t brdfType,
                               vec3& rayDirection, vec3& sampleWeight, float& volume_dis) {  // :649-729
+    note_margin(dot(geometryNormal, V));
     if (dot(geometryNormal, V) < 0.0f) return false;
     vec4 qRotationToZ = getRotationToZAxis(shadingNormal);
     vec3 Vlocal = rotatePoint(qRotationToZ, V);
@@ -350,6 +420,8 @@ bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, v
     } else if (brdfType == TRANSMISSION_TYPE) {
         if (material.volume) {
             const float refraction_ratio = material.frontFace ? 1.0f / material.ior : material.ior;
+            const float dn = dot(Nlocal, -Vlocal);
+            note_margin(1.0f - refraction_ratio * refraction_ratio * (1.0f - dn * dn));  // refract's k
             const vec3 refracted = refract(-Vlocal, Nlocal, refraction_ratio);
             if (refracted == vec3(0.0f)) {
                 sampleWeight = vec3(0.0f);
@@ -364,8 +436,8 @@ bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, v
         if (!material.frontFace && material.volume) {
             float dis = volume_dis;
             volume_dis = -1.0f;
-            vec3 sigma = log(material.attenuation_color) / material.attenuation_distance;
-            vec3 attenuation = exp(sigma * dis);
+            vec3 sigma = t_log(material.attenuation_color) / material.attenuation_distance;
+            vec3 attenuation = t_exp(sigma * dis);
             sampleWeight *= min(attenuation, vec3(1.0f));
         }
     }
@@ -376,6 +448,8 @@ bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, v
 
 vec3 evalCombinedBRDF(vec3 N, vec3 L, vec3 V, const MaterialBrdf& material) {  // PBR.glsl:731-745
     const BrdfData data = prepareBRDFData(N, L, V, material);
+    note_margin(dot(N, L));
+    note_margin(dot(N, V));
     if (data.Vbackfacing || data.Lbackfacing) return vec3(0.0f, 0.0f, 0.0f);
     vec3 specular = evalMicrofacet(data);
     vec3 diffuse = evalFrostbiteDisneyDiffuse(data);
@@ -1040,9 +1114,13 @@ bool anyhit_ignore(const orc_scene& s, uint32_t geo, uint32_t prim, uint32_t ins
         color4 = mix_vertex.color * diffuse_factor;
         opacity = color4.w;
     }
-    if (mat.alpha_mode == 2u) return (opacity < mat.alpha_cutoff);  // MASK
+    if (mat.alpha_mode == 2u) {  // MASK
+        if (ctx.tag != 0u) note_margin(opacity - mat.alpha_cutoff);  // camera rays are bit-exact
+        return (opacity < mat.alpha_cutoff);
+    }
     uvec4 key(ctx.px, ctx.py, ctx.sample, blend_hash(instance, prim, ctx.tag));  // D3
     float uu = uintToFloat(pcg4d(key).x);
+    if (ctx.tag != 0u) note_margin(opacity - uu);
     return (opacity <= uu);
 }
 
@@ -1050,6 +1128,10 @@ bool anyhit_ignore(const orc_scene& s, uint32_t geo, uint32_t prim, uint32_t ins
 vec3 sample_sky(const orc_scene& s, vec3 d) {
     if (s.sky_size == 0) return vec3(0.0f);
     float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    {  // face choice: distance between the largest and the second largest axis
+        const float hi = std::max(ax, std::max(ay, az)), lo = std::min(ax, std::min(ay, az));
+        note_margin(hi - (ax + ay + az - hi - lo));
+    }
     int face;
     float sc, tc, ma;
     if (ax >= ay && ax >= az) {
@@ -1110,6 +1192,7 @@ void miss_shader(FrameCtx& f, RayPayload& Ray, const float* dir) {
         for (size_t i = 0; i < s.dlights.size(); i++) {
             const gbrt_light_raw& li = s.dlights[i];
             float cos = dot(normalize(vec3(li.transform[0], li.transform[1], li.transform[2])), ray_direction);
+            note_margin(cos);
             if (cos < 0.0f) light_acc += -cos * vec3(li.color[0], li.color[1], li.color[2]) * li.intensity;
         }
     }
@@ -1163,11 +1246,14 @@ bool sampleLightRIS(const orc_scene& s, uvec4& rngState, vec3 hitPosition, vec3 
             vec3 lightVector = vec3(candidate.transform[0], candidate.transform[1], candidate.transform[2]) -
                                hitPosition;
             vec3 L = normalize(lightVector);
+            note_margin(dot(surfaceNormal, L) - 0.00001f);
             if (dot(surfaceNormal, L) < 0.00001f) continue;
             float candidatePdfG = luminance(getLightIntensityAtPoint(candidate, length(lightVector)));
             const float candidateRISWeight = candidatePdfG * candidateWeight;
             totalWeights += candidateRISWeight;
-            if (rand(rngState) < (candidateRISWeight / totalWeights)) {
+            const float accept = rand(rngState);
+            note_margin(accept - candidateRISWeight / totalWeights);
+            if (accept < (candidateRISWeight / totalWeights)) {
                 selectedSample = candidate;
                 samplePdfG = candidatePdfG;
             }
@@ -1225,6 +1311,10 @@ void closest_hit(FrameCtx& f, RayPayload& Ray, const HitT& hit, const float* wdi
     const bool frontFace = cos >= 0.0f;
     geo_normal = frontFace ? geo_normal : -geo_normal;
     const vec3 outwardNormal = dot(geo_normal, normal) < 0.0f ? -normal : normal;
+    if (f.bounce) {  // camera rays are bit-exact
+        note_margin(cos);
+        note_margin(dot(geo_normal, normal));
+    }
 
     vec3 emittance = vec3(mat.emissive_factor[0], mat.emissive_factor[1], mat.emissive_factor[2]);
     if (mat.emissive_texture.index >= 0)
@@ -1331,6 +1421,8 @@ void closest_hit(FrameCtx& f, RayPayload& Ray, const HitT& hit, const float* wdi
     } else {
         BRDFProb prob = getBrdfProbability(matbrdf, V, outwardNormal);
         float randfloat = rand(rngState);
+        note_margin(randfloat - prob.specular);
+        note_margin(randfloat - (prob.specular + prob.diffuse));
         if (randfloat < prob.specular) {
             brdfType = SPECULAR_TYPE;
             throughput /= prob.specular;
@@ -1455,6 +1547,7 @@ vec3 raygen_sample(FrameCtx& f, uint32_t x, uint32_t y, uint32_t W, uint32_t H, 
             primary->primitive_id = hit ? h.prim : ~0u;
             primary->custom_index = hit ? h.geo : ~0u;
         }
+        if (hit && b) note_edge(std::min(std::min(h.u, h.v), 1.0f - h.u - h.v));
         if (hit) closest_hit(f, Ray, h, d);
         else miss_shader(f, Ray, d);
         const vec3 hitColor = Ray.hitValue;
@@ -1469,6 +1562,7 @@ vec3 raygen_sample(FrameCtx& f, uint32_t x, uint32_t y, uint32_t W, uint32_t H, 
         if (b > 3u) {  // MIN_BOUNCES, rgen:15,108-118
             float rrProbability = clamp(luminance(throughput), 0.01f, 0.95f);
             float prop = rand(rngState);
+            note_margin(rrProbability - prop);
             if (rrProbability < prop) break;
             throughput /= rrProbability;
         }
@@ -1750,8 +1844,18 @@ int orc_trace(orc_scene* s, const gbrt_ray* rays, uint32_t n, uint32_t flags, gb
 int orc_render(orc_scene* s, const gbrt_ubo* ubo, uint32_t W, uint32_t H, uint32_t row0, uint32_t row1,
                float* accum, uint8_t* out, float* sample_radiance, gbrt_hit* primary_hits, int fp64, int nthreads,
                orc_stats* st) {
+    return orc_render_diag(s, ubo, W, H, row0, row1, accum, out, sample_radiance, primary_hits, nullptr, 0, fp64,
+                           nthreads, st);
+}
+
+int orc_render_diag(orc_scene* s, const gbrt_ubo* ubo, uint32_t W, uint32_t H, uint32_t row0, uint32_t row1,
+                    float* accum, uint8_t* out, float* sample_radiance, gbrt_hit* primary_hits, float* sample_margins,
+                    uint32_t nudge_ulps, int fp64, int nthreads, orc_stats* st) {
     if (!s->built) return GBRT_E_NOT_BUILT;
     if (row1 > H || row0 > row1) return GBRT_E_INVALID;
+#ifndef ORC_DIAG
+    if (sample_margins || nudge_ulps) return GBRT_E_INVALID;  // diagnostics live in liboracle_diag.so
+#endif
     auto t0 = std::chrono::steady_clock::now();
     const uint32_t ns = ubo->number_of_samples;
     const uint32_t sbase = ubo->total_number_of_samples - ns;
@@ -1776,8 +1880,19 @@ int orc_render(orc_scene* s, const gbrt_ubo* ubo, uint32_t W, uint32_t H, uint32
             float last_t = 0.0f;
             for (uint32_t si = 0; si < ns; ++si) {
                 gbrt_hit* ph = primary_hits ? &primary_hits[pix * ns + si] : nullptr;
+                SampleDiag diag{{INFINITY, INFINITY}, nudge_ulps, nudge_seed(x, y, sbase + si) ^ (nudge_ulps * 0x9E3779B9u)};
+#ifdef ORC_DIAG
+                g_diag = (sample_margins || nudge_ulps) ? &diag : nullptr;
+#endif
                 vec3 r = fp64 ? raygen_sample<double>(f, x, y, W, H, sbase + si, ph, cam, ext, last_t)
                               : raygen_sample<float>(f, x, y, W, H, sbase + si, ph, cam, ext, last_t);
+#ifdef ORC_DIAG
+                g_diag = nullptr;
+#endif
+                if (sample_margins) {
+                    sample_margins[(pix * ns + si) * 2] = diag.margin[0];
+                    sample_margins[(pix * ns + si) * 2 + 1] = diag.margin[1];
+                }
                 if (sample_radiance) {
                     float* sr = &sample_radiance[(pix * ns + si) * 3];
                     sr[0] = r.x; sr[1] = r.y; sr[2] = r.z;
@@ -1874,3 +1989,7 @@ void orc_sample_skybox(orc_scene* s, const float dir[3], float out[3]) {
 uint32_t orc_blend_hash(uint32_t instance, uint32_t prim, uint32_t tag) { return blend_hash(instance, prim, tag); }
 
 }  // extern "C"
+
+#ifdef ORC_DIAG
+float glsl::diag_round(float r) { return nudged(r); }
+#endif

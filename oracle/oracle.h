@@ -64,6 +64,18 @@ int  orc_render(orc_scene* s, const gbrt_ubo* ubo, uint32_t width, uint32_t heig
                 float* sample_radiance, gbrt_hit* primary_hits, int fp64, int nthreads,
                 orc_stats* st);
 
+/* orc_render plus parity diagnostics.  sample_margins (may be NULL) gets
+ * [pixel][sample][2] floats: [0] the smallest |operand - threshold| of the
+ * branch decisions the sample's path took, [1] the smallest barycentric of
+ * its secondary hits (both +inf when none).  nudge_ulps > 0 moves every
+ * transcendental result (sin, cos, pow, exp, log) by that many ulps, up or
+ * down by a per-sample hash, to expose samples that ulp-level arithmetic
+ * differences change. */
+int  orc_render_diag(orc_scene* s, const gbrt_ubo* ubo, uint32_t width, uint32_t height,
+                     uint32_t row0, uint32_t row1, float* accum, uint8_t* out_rgba8,
+                     float* sample_radiance, gbrt_hit* primary_hits, float* sample_margins,
+                     uint32_t nudge_ulps, int fp64, int nthreads, orc_stats* st);
+
 /* Shader-library entry points for known-answer tests. */
 void     orc_pcg4d(const uint32_t in[4], uint32_t out[4]);
 uint32_t orc_tea(uint32_t v0, uint32_t v1);

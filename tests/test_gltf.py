@@ -247,3 +247,31 @@ def test_loader_generates_tangents_for_normal_maps(tmp_path):
     json.dump(doc, open(path, "w"))
     mapped = gltf.load(str(path))
     assert np.allclose(mapped.vertices["tangent"][:4], [[1, 0, 0, 1]] * 4, atol=1e-6)
+
+
+def _asset_fixture():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_cornell_asset", os.path.join(os.path.dirname(__file__), "golden", "make_cornell_asset.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def test_cornell_asset_fixture():
+    """The committed fixture of the reference's Cornell box asset: the loader's
+    arrays, with a BLEND material (alpha_mode 3) and an emissive one; equal to
+    a fresh load when the reference checkout is on this machine."""
+    m = _asset_fixture()
+    sd = m.load()
+    assert sd.num_triangles == 16720 and len(sd.materials) == 9 and len(sd.instances) == 10
+    assert (sd.materials["alpha_mode"] == 3).sum() == 1 and not sd.fully_opaque
+    assert (sd.materials["emissive_factor"][:, :3].sum(1) > 0).sum() == 1
+    path = "/root/reference/assets/models/CornellBox/cornellBox.gltf"
+    if os.path.exists(path):
+        fresh = gltf.load(path)
+        for k in ("vertices", "indices", "prims", "materials", "geo_ranges", "instances", "plights"):
+            assert np.array_equal(getattr(fresh, k).view(np.uint8), getattr(sd, k).view(np.uint8)), k
+    import pyoracle as O
+    r = O.OracleScene(sd).render(sd.ubo(32, 32, samples=2, bounces=6, exposure=5.0), 32, 32, want_samples=True)
+    assert np.all(np.isfinite(r["samples"])) and r["samples"].max() > 0

@@ -260,3 +260,65 @@ def test_injected_admission_failure():
             assert np.array_equal(a.download(), acc_ref)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("seed", [1, 4, 12])
+def test_batched_scene_jobs_vs_oracle(gpu_ctx, seed):
+    """Scenes of the batched configuration (seeded instanced tori: FP16 MASK
+    alpha textures, transmissive materials with a volume and random IOR,
+    three point lights), capped at 60k triangles so the oracle builds them
+    quickly: submitted as jobs beside another job, each job's accumulation
+    and image equal the solo render's bit for bit, and the solo render meets
+    the per-sample parity contract against the oracle (primary hits
+    bit-exact)."""
+    import parity
+    import pyoracle as O
+    from rustracer_gb300 import gbrt, types as T, workloads
+    sd, _, _, _ = workloads.batched_scene(seed, max_tri=60_000, min_tri=1_000)
+    assert (sd.materials["alpha_mode"] == T.ALPHA_MASK).any() and (sd.materials["transmission_exist"] == 1).any()
+    W, H = 96, 64
+    ubo = sd.ubo(W, H, samples=4, bounces=8, exposure=1.0)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    acc_solo = gbrt.Accum(gpu_ctx, W, H)
+    solo = sc.render(ubo, acc_solo, want_samples=True, want_hits=True, mode=gbrt.MODE_WAVEFRONT)
+    orc = O.OracleScene(sd, diag=True)
+    ref = orc.render(ubo, W, H, want_samples=True, want_hits=True, want_margins=True)
+    for f in ("instance_id", "primitive_id"):
+        assert np.array_equal(solo["hits"][f], ref["hits"][f]), f
+    assert np.array_equal(solo["hits"]["t"].view(np.uint32), ref["hits"]["t"].view(np.uint32))
+    parity.assert_samples(solo["samples"], ref, orc, ubo, W, H)
+    other = scenes.icosphere_scene(subdiv=3)
+    sc2 = gbrt.Scene(gpu_ctx, other)
+    acc, acc2 = gbrt.Accum(gpu_ctx, W, H), gbrt.Accum(gpu_ctx, 200, 120)
+    j2 = gpu_ctx.submit(sc2, other.ubo(200, 120, samples=3, bounces=6, exposure=1.0), acc2)
+    j = gpu_ctx.submit(sc, ubo, acc)
+    assert j.wait()["status"] == 0 and j2.wait()["status"] == 0
+    assert np.array_equal(acc.download(), acc_solo.download())
+    assert np.array_equal(j.image.reshape(H, W, 4), solo["image"])
+
+
+def test_serving_skinned_job_vs_oracle(gpu_ctx):
+    """The serving pool's skinned scene (a tube on a 64-bone chain in the
+    Cornell box): a job carrying its joint matrices skins, refits and renders;
+    its result equals skin-then-render, whose samples meet the contract
+    against the oracle skinned with the same matrices."""
+    import parity
+    import pyoracle as O
+    from rustracer_gb300 import gbrt, workloads
+    sd = workloads.skinned_scene(rings=40, segments=24)
+    skins = zoo.bone_matrices(sd.bones, 1.1)
+    W, H = 80, 64
+    ubo = sd.ubo(W, H, samples=4, bounces=6, exposure=1.0)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    acc = gbrt.Accum(gpu_ctx, W, H)
+    j = gpu_ctx.submit(sc, ubo, acc, skins=skins)
+    assert j.wait()["status"] == 0
+    sc.skin_and_refit(skins)
+    acc_solo = gbrt.Accum(gpu_ctx, W, H)
+    solo = sc.render(ubo, acc_solo, want_samples=True, want_hits=True, mode=gbrt.MODE_WAVEFRONT)
+    assert np.array_equal(acc.download(), acc_solo.download())
+    orc = O.OracleScene(sd, diag=True)
+    orc.skin(skins)
+    ref = orc.render(ubo, W, H, want_samples=True, want_hits=True, want_margins=True)
+    assert np.array_equal(solo["hits"]["primitive_id"], ref["hits"]["primitive_id"])
+    parity.assert_samples(solo["samples"], ref, orc, ubo, W, H)

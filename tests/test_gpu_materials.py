@@ -5,8 +5,7 @@
   texture, BLEND from vertex alpha, specular-glossiness, transmission with a
   volume, KHR_materials_specular, unlit, point + directional lights and a
   skybox -- primary hits bit-exact, per-sample radiance within the render
-  contract (1e-4 relative, a small share of branch flips), in both the
-  megakernel and the wavefront.
+  contract of tests/parity.py, in both the megakernel and the wavefront.
 * skinning (AnimationCompute.comp): after gbrt_skin_and_refit the GPU's
   hits on the skinned tube are bit-identical to the oracle's hits on its own
   skinned vertices, for two consecutive animation frames.
@@ -14,34 +13,25 @@
 import numpy as np
 import pytest
 
+import parity
 from rustracer_gb300 import scenes, zoo
 
 pytestmark = pytest.mark.gpu
-
-REL_TOL = 1e-4
-ABS_TOL = 1e-6
-
-
-def flip_share(a, b):
-    a, b = a.reshape(-1, 3).astype(np.float64), b.reshape(-1, 3).astype(np.float64)
-    assert np.all(np.isfinite(a))
-    ok = np.all(np.abs(a - b) <= REL_TOL * np.maximum(np.abs(a), np.abs(b)) + ABS_TOL, axis=1)
-    return 1.0 - ok.mean()
-
 
 @pytest.fixture(scope="module")
 def zoo_ref():
     import pyoracle as O
     sd = zoo.material_zoo()
     ubo = sd.ubo(96, 96, samples=8, bounces=8, exposure=1.0, has_sky=True)
-    ref = O.OracleScene(sd).render(ubo, 96, 96, want_samples=True, want_hits=True)
-    return sd, ubo, ref
+    orc = O.OracleScene(sd, diag=True)
+    ref = orc.render(ubo, 96, 96, want_samples=True, want_hits=True, want_margins=True)
+    return sd, ubo, ref, orc
 
 
 @pytest.mark.parametrize("mode", [1, 2], ids=["megakernel", "wavefront"])
 def test_material_zoo(gpu_ctx, zoo_ref, mode):
     from rustracer_gb300 import gbrt
-    sd, ubo, ref = zoo_ref
+    sd, ubo, ref, orc = zoo_ref
     sc = gbrt.Scene(gpu_ctx, sd)
     acc = gbrt.Accum(gpu_ctx, 96, 96)
     r = sc.render(ubo, acc, want_samples=True, want_hits=True, mode=mode)
@@ -52,8 +42,7 @@ def test_material_zoo(gpu_ctx, zoo_ref, mode):
     # every material sphere is on screen
     prims = set(np.unique(gh["primitive_id"][gh["primitive_id"] >= 0]).tolist())
     assert len(prims) > 500
-    flips = flip_share(r["samples"], ref["samples"])
-    assert flips <= 5e-3, flips
+    parity.assert_samples(r["samples"], ref, orc, ubo, 96, 96)
     diff = np.abs(r["image"].astype(int) - ref["image"].astype(int))
     assert (diff <= 1).mean() > 0.98
 
@@ -100,14 +89,14 @@ def test_skinned_tube_render(gpu_ctx):
     sd = zoo.skinned_tube()
     skins = zoo.bone_matrices(sd.bones, 1.3)
     ubo = sd.ubo(64, 64, samples=4, bounces=6, exposure=1.0)
-    orc = O.OracleScene(sd)
+    orc = O.OracleScene(sd, diag=True)
     orc.skin(skins)
-    ref = orc.render(ubo, 64, 64, want_samples=True, want_hits=True)
+    ref = orc.render(ubo, 64, 64, want_samples=True, want_hits=True, want_margins=True)
     sc = gbrt.Scene(gpu_ctx, sd)
     sc.skin_and_refit(skins)
     r = sc.render(ubo, gbrt.Accum(gpu_ctx, 64, 64), want_samples=True, want_hits=True, mode=2)
     assert np.array_equal(r["hits"]["primitive_id"], ref["hits"]["primitive_id"])
-    assert flip_share(r["samples"], ref["samples"]) <= 5e-3
+    parity.assert_samples(r["samples"], ref, orc, ubo, 64, 64)
 
 
 def test_refit_drift_triggers_rebuild(gpu_ctx):

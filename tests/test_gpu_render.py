@@ -1,34 +1,36 @@
 """GPU path tracing vs the CPU oracle through gbrt_render_ex.
 
-Contract (per sample, D1 seeding makes every sample depend only on its
-pixel and global sample index):
+Contract (per sample; D1 seeding makes every sample depend only on its pixel
+and global sample index), asserted by tests/parity.py:
 * primary-ray hits are bit-identical;
 * per-sample radiance agrees within 1e-4 relative (|a-b| <= 1e-4 *
-  max(|a|, |b|) + 1e-6) except for samples whose path took a different
-  branch because a transcendental (sin/cos/pow/exp/log) differed by an ulp
-  between CUDA and libm -- at most FLIP_MAX of the samples.
+  max(|a|, |b|) + 1e-6), except samples the oracle shows to be
+  ill-conditioned at the ulp level (a branch decision within 2^-14 of its
+  threshold, a secondary hit within 2^-14 of a triangle edge, or a sample
+  that leaves the band itself when the oracle's transcendentals and dot
+  products move by 1-3 ulps); no other mismatch is allowed, and at most
+  0.2% of the samples may mismatch at all.
 """
 import os
 
 import numpy as np
 import pytest
 
+import parity
 from rustracer_gb300 import scenes, types as T
 
 pytestmark = pytest.mark.gpu
 
-REL_TOL = 1e-4
-ABS_TOL = 1e-6
-FLIP_MAX = 2e-3
+FLIP_MAX = parity.FLIP_MAX
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
-def compare_samples(gpu, ref):
-    a, b = gpu.reshape(-1, 3).astype(np.float64), ref.reshape(-1, 3).astype(np.float64)
-    ok = np.all(np.abs(a - b) <= REL_TOL * np.maximum(np.abs(a), np.abs(b)) + ABS_TOL, axis=1)
-    assert np.all(np.isfinite(a)), "non-finite GPU radiance"
-    return 1.0 - ok.mean()
+def oracle_ref(sd, ubo, w, h, rows=None):
+    """The oracle (diagnostics build) with samples, hits and margins."""
+    import pyoracle as O
+    orc = O.OracleScene(sd, diag=True)
+    return orc, orc.render(ubo, w, h, rows=rows, want_samples=True, want_hits=True, want_margins=True)
 
 
 def render_gpu(ctx, sd, ubo, w, h, mode=0, **kw):
@@ -41,39 +43,43 @@ def render_gpu(ctx, sd, ubo, w, h, mode=0, **kw):
 def test_golden_cornell_32(gpu_ctx):
     g = np.load(os.path.join(GOLDEN, "golden_cornell_32.npz"))
     ubo = np.frombuffer(g["ubo"].tobytes(), T.UBO)[0]
-    r = render_gpu(gpu_ctx, scenes.cornell(), ubo, 32, 32)
+    sd = scenes.cornell()
+    orc, ref = oracle_ref(sd, ubo, 32, 32)
+    assert np.array_equal(ref["samples"].view(np.uint32), g["samples"].view(np.uint32))  # the fixture is the oracle's
+    r = render_gpu(gpu_ctx, sd, ubo, 32, 32)
     h, gh = r["hits"].reshape(-1), g["hits"].reshape(-1)
     assert np.array_equal(h["primitive_id"], gh["primitive_id"])
     assert np.array_equal(h["t"].view(np.uint32), gh["t"].view(np.uint32))
-    assert compare_samples(r["samples"], g["samples"]) <= FLIP_MAX * 4
+    parity.assert_samples(r["samples"], ref, orc, ubo, 32, 32)
 
 
 def test_golden_ico2(gpu_ctx):
     g = np.load(os.path.join(GOLDEN, "golden_ico2.npz"))
     ubo = np.frombuffer(g["ubo"].tobytes(), T.UBO)[0]
-    r = render_gpu(gpu_ctx, scenes.icosphere_scene(subdiv=2), ubo, 24, 16)
+    sd = scenes.icosphere_scene(subdiv=2)
+    orc, ref = oracle_ref(sd, ubo, 24, 16)
+    assert np.array_equal(ref["samples"].view(np.uint32), g["samples"].view(np.uint32))
+    r = render_gpu(gpu_ctx, sd, ubo, 24, 16)
     assert np.array_equal(r["hits"]["primitive_id"], g["hits"]["primitive_id"])
-    assert compare_samples(r["samples"], g["samples"]) <= 0.02
+    parity.assert_samples(r["samples"], ref, orc, ubo, 24, 16)
 
 
 @pytest.mark.parametrize("mode", [1, 2], ids=["megakernel", "wavefront"])
 def test_cornell_256_16spp(gpu_ctx, mode):
     """Config 1: 256x256, 16 spp, depth 8, pinhole fov 40, AA on."""
-    import pyoracle as O
     sd = scenes.cornell()
     ubo = sd.ubo(256, 256, samples=16, bounces=8, exposure=1.0)
-    ref = O.OracleScene(sd).render(ubo, 256, 256, want_samples=True, want_hits=True)
+    orc, ref = oracle_ref(sd, ubo, 256, 256)
     r = render_gpu(gpu_ctx, sd, ubo, 256, 256, mode=mode)
     gh, rh = r["hits"].reshape(-1), ref["hits"].reshape(-1)
     for f in ("instance_id", "primitive_id"):
         assert np.array_equal(gh[f], rh[f]), f
     assert np.array_equal(gh["t"].view(np.uint32), rh["t"].view(np.uint32))
-    flips = compare_samples(r["samples"], ref["samples"])
-    assert flips <= FLIP_MAX, flips
+    parity.assert_samples(r["samples"], ref, orc, ubo, 256, 256)
     # ray counts agree up to flipped paths
     st, rs = r["stats"], ref["stats"]
     assert st["rays_camera"] == rs["rays_camera"] == 256 * 256 * 16
-    assert abs(int(st["rays_extension"]) - int(rs["rays_extension"])) <= 0.01 * rs["rays_extension"]
+    assert abs(int(st["rays_extension"]) - int(rs["rays_extension"])) <= 0.002 * rs["rays_extension"]
     # tone-mapped image within one code value on almost every pixel
     diff = np.abs(r["image"].astype(int) - ref["image"].astype(int))
     assert (diff <= 1).mean() > 0.99
@@ -83,15 +89,41 @@ def test_cornell_256_16spp(gpu_ctx, mode):
 def test_icosphere_nee(gpu_ctx, mode):
     """Point lights exercise NEE (sampleLightRIS + shadow rays) and the
     metallic-roughness BRDF."""
-    import pyoracle as O
     sd = scenes.icosphere_scene(subdiv=4)
     ubo = sd.ubo(96, 64, samples=4, bounces=8, exposure=1.0)
-    ref = O.OracleScene(sd).render(ubo, 96, 64, want_samples=True, want_hits=True)
+    orc, ref = oracle_ref(sd, ubo, 96, 64)
     r = render_gpu(gpu_ctx, sd, ubo, 96, 64, mode=mode)
     assert np.array_equal(r["hits"]["primitive_id"], ref["hits"]["primitive_id"])
     assert ref["stats"]["rays_shadow"] > 0
-    assert abs(int(r["stats"]["rays_shadow"]) - int(ref["stats"]["rays_shadow"])) <= 0.01 * ref["stats"]["rays_shadow"]
-    assert compare_samples(r["samples"], ref["samples"]) <= 0.01
+    assert abs(int(r["stats"]["rays_shadow"]) - int(ref["stats"]["rays_shadow"])) <= 0.002 * ref["stats"]["rays_shadow"]
+    parity.assert_samples(r["samples"], ref, orc, ubo, 96, 64)
+
+
+@pytest.mark.parametrize("band", [(508, 572), (120, 152)], ids=["middle", "upper"])
+def test_headline_frame_band(gpu_ctx, band):
+    """The bench's own workload: the icosphere of subdivision 7 (327,714
+    triangles, 24 random metallic-roughness materials, 4 point lights) at
+    1920x1080, depth 8, with the bench's tuning (8-wide BVH, ray-sort key).
+    The GPU renders the full frame at 2 spp; a band of full-width rows is
+    compared with the oracle: primary hits bit-exact, per-sample radiance
+    within the contract."""
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=7)
+    W, H = 1920, 1080
+    ubo = sd.ubo(W, H, samples=2, bounces=8, exposure=1.0)
+    orc, ref = oracle_ref(sd, ubo, W, H, rows=band)
+    sc = gbrt.Scene(gpu_ctx, sd)
+    sc.set_tuning(width=8, sort_rays=True)
+    r = sc.render(ubo, gbrt.Accum(gpu_ctx, W, H), want_samples=True, want_hits=True, mode=gbrt.MODE_WAVEFRONT)
+    r0, r1 = band
+    gh = r["hits"].reshape(H, W, 2)[r0:r1]
+    rh = ref["hits"].reshape(H, W, 2)[r0:r1]
+    for f in ("instance_id", "primitive_id"):
+        assert np.array_equal(gh[f], rh[f]), f
+    assert np.array_equal(gh["t"].view(np.uint32), rh["t"].view(np.uint32))
+    assert (rh["primitive_id"] != 0xFFFFFFFF).mean() > 0.4
+    c = parity.assert_samples(r["samples"].reshape(H, W, 2, 3)[r0:r1], ref, orc, ubo, W, H, rows=band)
+    assert c["n"] == (r1 - r0) * W * 2
 
 
 def test_accumulation_across_frames(gpu_ctx):
@@ -110,7 +142,6 @@ def test_accumulation_across_frames(gpu_ctx):
 def test_sky_and_dir_light(gpu_ctx):
     """Miss shader: directional light term on secondary misses and the
     skybox (RayTracing.rmiss:18-37)."""
-    import pyoracle as O
     sd = scenes.cornell()
     rng = np.random.default_rng(3)
     sd.skybox = (8, rng.integers(0, 256, 6 * 8 * 8 * 4).astype(np.uint8))
@@ -120,9 +151,9 @@ def test_sky_and_dir_light(gpu_ctx):
     sd.dlights = np.array([d], T.LIGHT)
     ubo = sd.ubo(64, 64, samples=4, bounces=6, exposure=1.0, has_sky=True, eye=(0.3, 0.2, 3.8),
                  direction=(0.3, 0.1, -1.0))
-    ref = O.OracleScene(sd).render(ubo, 64, 64, want_samples=True)
+    orc, ref = oracle_ref(sd, ubo, 64, 64)
     r = render_gpu(gpu_ctx, sd, ubo, 64, 64)
-    assert compare_samples(r["samples"], ref["samples"]) <= FLIP_MAX * 5
+    parity.assert_samples(r["samples"], ref, orc, ubo, 64, 64)
 
 
 def test_wavefront_matches_megakernel(gpu_ctx):
@@ -133,7 +164,7 @@ def test_wavefront_matches_megakernel(gpu_ctx):
     a = render_gpu(gpu_ctx, sd, ubo, 160, 90, mode=1)
     b = render_gpu(gpu_ctx, sd, ubo, 160, 90, mode=2)
     assert np.array_equal(a["hits"], b["hits"])
-    assert compare_samples(b["samples"], a["samples"]) <= FLIP_MAX
+    assert parity.mismatched(b["samples"], a["samples"]).mean() <= FLIP_MAX
     for f in ("rays_camera", "rays_extension", "rays_shadow"):
         assert abs(int(a["stats"][f]) - int(b["stats"][f])) <= 0.002 * int(a["stats"][f]) + 2, f
 
@@ -180,15 +211,14 @@ def test_async_frames_equal_sync(gpu_ctx):
 def test_hdr_float_skybox(gpu_ctx):
     """An RGBA32F (linear, HDR: texels up to 20) skybox through
     gbrt_skybox_set_ex: per-sample radiance matches the oracle's."""
-    import pyoracle as O
     sd = scenes.icosphere_scene(subdiv=2)
     rng = np.random.default_rng(4)
     sd.skybox = (8, (rng.random(6 * 8 * 8 * 4) * 20.0).astype(np.float32))
     ubo = sd.ubo(64, 48, samples=4, bounces=6, exposure=1.0, has_sky=True, eye=(0.3, 0.2, 3.8),
                  direction=(0.3, 0.1, -1.0))
-    ref = O.OracleScene(sd).render(ubo, 64, 48, want_samples=True)
+    orc, ref = oracle_ref(sd, ubo, 64, 48)
     r = render_gpu(gpu_ctx, sd, ubo, 64, 48)
-    assert compare_samples(r["samples"], ref["samples"]) <= FLIP_MAX * 5
+    parity.assert_samples(r["samples"], ref, orc, ubo, 64, 48)
 
 
 def test_converged_vs_fp64_reference(gpu_ctx):
@@ -242,16 +272,15 @@ def test_white_furnace(gpu_ctx):
     0.5 it grows (1 < mean < 1 / (1 - 0.75), the largest per-bounce weight of
     the reference's lobes at roughness 1); the GPU meets the per-sample parity
     contract against the oracle in both."""
-    import pyoracle as O
     for albedo, lo, hi in ((0.0, 1.0, 1.1), (0.5, 1.05, 4.0)):
         sd = _furnace(albedo)
         ubo = sd.ubo(32, 32, samples=4, bounces=8, exposure=1.0)
-        ref = O.OracleScene(sd).render(ubo, 32, 32, want_samples=True)
+        orc, ref = oracle_ref(sd, ubo, 32, 32)
         r = render_gpu(gpu_ctx, sd, ubo, 32, 32)
         s = r["samples"]
         assert s.min() >= 1.0 and ref["samples"].min() >= 1.0
         assert lo <= float(s.mean()) < hi, (albedo, float(s.mean()))
-        assert compare_samples(s, ref["samples"]) <= FLIP_MAX
+        parity.assert_samples(s, ref, orc, ubo, 32, 32)
 
 
 def test_checkpoint_resume(gpu_ctx, tmp_path):
