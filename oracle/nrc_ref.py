@@ -10,6 +10,11 @@ differences in tests).  The cache has no counterpart in the reference, so
 there is nothing to pin it to beyond its own published definition
 (Mueller et al. 2022 encoding, Mueller et al. 2021 loss): parity with the
 GPU is the check.
+
+loss_and_grads(..., bf16=True) follows the library's tensor-core training:
+every matrix operand (encoding, activations, weights, dL/dy and the
+pre-activation gradients) is rounded to BF16 (round to nearest even) where
+the kernels round it, and the products are summed in float64.
 """
 import numpy as np
 
@@ -86,7 +91,31 @@ def forward(mlp_flat, grid, p01, levels, log2_table):
     return y, (idx, w, hs, Ws)
 
 
-def loss_and_grads(mlp_flat, grid, p01, target, levels, log2_table):
+def bf16(x):
+    """Rounds to BF16 (nearest even) through float32, returned as float64."""
+    f = np.asarray(x, np.float64).astype(np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward_bf16(mlp_flat, grid, p01, levels, log2_table):
+    """The forward pass with BF16 operands: H_0 = bf16(encoding), H_{l+1} =
+    bf16(relu(H_l bf16(W_l)^T)), y = H_5 bf16(W_5)^T."""
+    idx, w = encode_corners(p01, levels, log2_table)
+    g2 = np.asarray(grid, np.float64).reshape(-1, 2)
+    x = np.einsum("nlc,nlcf->nlf", w, g2[idx]).reshape(len(p01), 32)
+    Ws = [bf16(W) for W in unpack_mlp(mlp_flat)]
+    hs = [bf16(x)]
+    for l in range(LAYERS):
+        hs.append(bf16(np.maximum(hs[-1] @ Ws[l].T, 0.0)))
+    y = hs[LAYERS] @ Ws[LAYERS].T
+    return y, (idx, w, hs, Ws)
+
+
+def loss_and_grads(mlp_flat, grid, p01, target, levels, log2_table, bf16_ops=False):
+    if bf16_ops:
+        return _loss_and_grads_bf16(mlp_flat, grid, p01, target, levels, log2_table)
     y, (idx, w, hs, Ws) = forward(mlp_flat, grid, p01, levels, log2_table)
     n = len(p01)
     t = np.asarray(target, np.float64)[:, :3]
@@ -100,6 +129,27 @@ def loss_and_grads(mlp_flat, grid, p01, target, levels, log2_table):
     for l in range(LAYERS - 1, 0, -1):
         gW[l] = dz.T @ hs[l]
         dz = (dz @ Ws[l]) * (hs[l] > 0)
+    gW[0] = dz.T @ hs[0]
+    dx = (dz @ Ws[0]).reshape(n, LEVELS, 2)
+    ggrid = np.zeros(np.asarray(grid).size, np.float64).reshape(-1, 2)
+    np.add.at(ggrid, idx.reshape(-1), (w[..., None] * dx[:, :, None, :]).reshape(-1, 2))
+    return loss, np.concatenate([g.reshape(-1) for g in gW]), ggrid.reshape(-1)
+
+
+def _loss_and_grads_bf16(mlp_flat, grid, p01, target, levels, log2_table):
+    y, (idx, w, hs, Ws) = forward_bf16(mlp_flat, grid, p01, levels, log2_table)
+    n = len(p01)
+    t = np.asarray(target, np.float64)[:, :3]
+    d = y - t
+    den = y * y + 0.01
+    loss = float(np.sum(d * d / den) / (n * 3))
+    dy = bf16(2.0 * d / den / (3 * n))
+    gW = [None] * (LAYERS + 1)
+    gW[LAYERS] = dy.T @ hs[LAYERS]
+    dz = bf16((dy @ Ws[LAYERS]) * (hs[LAYERS] > 0))
+    for l in range(LAYERS - 1, 0, -1):
+        gW[l] = dz.T @ hs[l]
+        dz = bf16((dz @ Ws[l]) * (hs[l] > 0))
     gW[0] = dz.T @ hs[0]
     dx = (dz @ Ws[0]).reshape(n, LEVELS, 2)
     ggrid = np.zeros(np.asarray(grid).size, np.float64).reshape(-1, 2)

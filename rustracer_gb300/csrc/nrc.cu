@@ -536,6 +536,335 @@ __global__ void __launch_bounds__(256) nrc_wgrad_kernel(const float* __restrict_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Training on tensor cores (the default; GBRT_NRC_TRAIN_FP32 keeps the FP32
+// kernels above).  BF16 operands, FP32 accumulation, mma.sync m16n8k16:
+// * nrc_train_tc_kernel: a warp takes 32 samples: FP32 encoding from the
+//   master table (lane = sample), the forward pass layer by layer as in the
+//   queries (accumulators -> ReLU -> BF16 A fragments in registers), the loss
+//   and dL/dy in FP32, then the backward pass dH_l = dZ_{l+1} W_l on the
+//   tensor cores with the transposed BF16 weights, the ReLU masks read back
+//   from the stored activations; the encoding gradient is scattered into the
+//   table gradient with float2 atomics.  Activations H_0..H_5 and
+//   pre-activation gradients dZ_1..dZ_5, dY are written in BF16, sample-major;
+// * nrc_wgrad_tc_kernel: dW_l = dZ_{l+1}^T H_l over the batch, split-K over
+//   samples: tiles of 64 samples staged in shared memory, operands loaded
+//   transposed with ldmatrix.trans, partial sums added with atomics.
+// The float64 oracle reproduces these roundings (oracle/nrc_ref.py, bf16).
+// ---------------------------------------------------------------------------
+constexpr int kTActStride = kNrcIn + kNrcHiddenLayers * kNrcHidden;  // 352 BF16: H0 | H1..H5
+constexpr int kTGradStride = kNrcHiddenLayers * kNrcHidden + 16;     // 336 BF16: dZ1..dZ5 | dY (3, padded to 16)
+__host__ __device__ constexpr int bwd_out_pad(int l) { return l == 5 ? 16 : kNrcHidden; }
+// transposed BF16 weights W_l^T [in][out padded + 8], layer offsets
+__host__ __device__ constexpr int bwd_off(int l) {
+    return l == 0 ? 0 : bwd_off(l - 1) + in_dim(l - 1) * (bwd_out_pad(l - 1) + kPadK);
+}
+constexpr int kBwdElems = bwd_off(6);  // 22272
+constexpr int kTrainWarps = 4;
+constexpr int kXRow = kNrcIn + 1;  // FP32 row of the encoding-gradient staging tile
+constexpr size_t kTrainTcSmem =
+    (size_t)(kBf16Padded + kBwdElems) * 2 + (size_t)kTrainWarps * 32 * kXRow * 4;
+
+// Every element of the transposed copy, zero in the padding (the dY
+// padding columns multiply it).
+__global__ void nrc_bwd_weights_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ wt) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kBwdElems) return;
+    int l = 0;
+    while (l < 5 && e >= bwd_off(l + 1)) ++l;
+    const int row = (e - bwd_off(l)) / (bwd_out_pad(l) + kPadK), col = (e - bwd_off(l)) % (bwd_out_pad(l) + kPadK);
+    const float x = col < out_dim(l) ? w[f32_off(l) + col * in_dim(l) + row] : 0.0f;  // W_l[o = col][k = row]
+    wt[e] = __float2bfloat16_rn(x);
+}
+
+// The 16 x (8 NT) accumulators of rows m*16 + {g, g + 8} as BF16 A-fragment
+// words, stored at row-major BF16 offset `col0` of each sample's row.
+GB_D void store_frag_rows(uint32_t* dst_row0, uint32_t base, uint32_t n, int stride_words, int col0,
+                          const uint32_t (&a)[2][4][4], int nk, int g, int t) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t row = base + m * 16 + g + h * 8;
+            if (row >= n) continue;
+            uint32_t* r = dst_row0 + (size_t)row * stride_words + col0 / 2;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (j >= nk) break;
+                r[j * 8 + t] = a[m][j][h];          // cols 16 j + 2 t, + 1
+                r[j * 8 + 4 + t] = a[m][j][2 + h];  // cols 16 j + 8 + 2 t, + 1
+            }
+        }
+}
+
+// dZ = dH * [H > 0] in the accumulator layout, H read back as BF16 pairs
+// from the stored activations (rows past n: H = 0), then packed as A
+// fragments.
+GB_D void mask_to_a(const float (&acc)[2][8][4], const uint32_t* act_row0, uint32_t base, uint32_t n, int hcol0,
+                    uint32_t (&a)[2][4][4], int g, int t) {
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        uint32_t hw[2][8];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t row = base + m * 16 + g + h * 8;
+            const uint32_t* r = act_row0 + (size_t)row * (kTActStride / 2) + hcol0 / 2;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) hw[h][nt] = row < n ? r[nt * 4 + t] : 0u;
+        }
+        float d[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                // BF16 halves: low 16 bits = col 2t, high = col 2t + 1; positive iff > 0
+                const uint32_t lo = hw[h][nt] & 0xFFFFu, hi = hw[h][nt] >> 16;
+                d[nt][2 * h] = (lo != 0u && !(lo & 0x8000u)) ? acc[m][nt][2 * h] : 0.0f;
+                d[nt][2 * h + 1] = (hi != 0u && !(hi & 0x8000u)) ? acc[m][nt][2 * h + 1] : 0.0f;
+            }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            a[m][j][0] = pack_bf16(d[2 * j][0], d[2 * j][1]);
+            a[m][j][1] = pack_bf16(d[2 * j][2], d[2 * j][3]);
+            a[m][j][2] = pack_bf16(d[2 * j + 1][0], d[2 * j + 1][1]);
+            a[m][j][3] = pack_bf16(d[2 * j + 1][2], d[2 * j + 1][3]);
+        }
+    }
+}
+
+struct NrcTcGrad {
+    float* grid;            // [levels * table * 2]
+    float* loss;            // one word
+    uint32_t* act;          // [n][kTActStride / 2] BF16 pairs
+    uint32_t* dz;           // [n][kTGradStride / 2] BF16 pairs
+};
+
+__global__ void __launch_bounds__(kTrainWarps * 32)
+    nrc_train_tc_kernel(NrcView v, NrcTcGrad gr, const __nv_bfloat16* __restrict__ wbwd, const float4* __restrict__ pos,
+                        const float4* __restrict__ target, uint32_t n, float inv_n) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __nv_bfloat16* swf = reinterpret_cast<__nv_bfloat16*>(smem);  // forward weights, padded rows
+    __nv_bfloat16* swb = swf + kBf16Padded;                        // transposed weights
+    float* sx_all = reinterpret_cast<float*>(swb + kBwdElems);
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(v.mlp_h);
+        uint4* dst = reinterpret_cast<uint4*>(swf);
+        for (int i = threadIdx.x; i < kBf16Padded / 8; i += blockDim.x) dst[i] = src[i];
+        src = reinterpret_cast<const uint4*>(wbwd);
+        dst = reinterpret_cast<uint4*>(swb);
+        for (int i = threadIdx.x; i < kBwdElems / 8; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float* sx = sx_all + warp * 32 * kXRow;
+    __nv_bfloat16* sin = reinterpret_cast<__nv_bfloat16*>(sx);  // the BF16 encoding tile shares it (32 x 40)
+    float loss = 0.0f;
+    for (uint32_t base = (blockIdx.x * kTrainWarps + warp) * 32u; base < n; base += gridDim.x * kTrainWarps * 32u) {
+        const uint32_t i = base + lane;
+        float3 p = f3(0.0f);
+        {  // encoding from the FP32 master table, lane = sample
+            float x[kNrcIn];
+            if (i < n) {
+                p = nrc_normalise(v, f3(pos[i]));
+#pragma unroll
+                for (int l = 0; l < kNrcLevels; ++l) {
+                    float f0 = 0.0f, f1 = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        uint32_t idx;
+                        float w;
+                        nrc_corner(v, l, p, c, idx, w);
+                        const float2 e = reinterpret_cast<const float2*>(v.grid_w)[idx];
+                        f0 = fmaf(w, e.x, f0);
+                        f1 = fmaf(w, e.y, f1);
+                    }
+                    x[2 * l] = f0;
+                    x[2 * l + 1] = f1;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < kNrcIn; ++k) x[k] = 0.0f;
+            }
+            uint32_t* arow = i < n ? gr.act + (size_t)i * (kTActStride / 2) : nullptr;
+#pragma unroll
+            for (int k = 0; k < kNrcIn; k += 2) {
+                const uint32_t pk = pack_bf16(x[k], x[k + 1]);
+                *reinterpret_cast<uint32_t*>(sin + lane * kInRow + k) = pk;
+                if (arow) arow[k / 2] = pk;
+            }
+        }
+        __syncwarp();
+        uint32_t a[2][4][4];
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+                const __nv_bfloat16* r0 = sin + (m * 16 + g) * kInRow + ks * 16 + t * 2;
+                const __nv_bfloat16* r1 = r0 + 8 * kInRow;
+                a[m][ks][0] = *reinterpret_cast<const uint32_t*>(r0);
+                a[m][ks][1] = *reinterpret_cast<const uint32_t*>(r1);
+                a[m][ks][2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+                a[m][ks][3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+            }
+        __syncwarp();
+        // forward
+        float acc[2][8][4];
+#pragma unroll 1
+        for (int l = 0; l < kNrcHiddenLayers; ++l) {
+            if (l == 0) mlp_layer<kNrcIn, 8>(swf + bf16_off(0), a, acc, g, t);
+            else mlp_layer<kNrcHidden, 8>(swf + bf16_off(l), a, acc, g, t);
+            relu_to_a(acc, a);
+            store_frag_rows(gr.act, base, n, kTActStride / 2, kNrcIn + l * kNrcHidden, a, 4, g, t);
+        }
+        mlp_layer<kNrcHidden, 1>(swf + bf16_off(5), a, acc, g, t);
+        // loss and dL/dy (columns 0..2 of the output tile: t = 0 holds 0, 1; t = 1 holds 2)
+        uint32_t ady[2][4][4];
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            float dy[4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t row = base + m * 16 + g + h * 8;
+                const float4 tg = (row < n && t < 2) ? target[row] : f4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int col = 2 * t + q;
+                    float d = 0.0f;
+                    if (row < n && col < kNrcOut) {
+                        const float y = acc[m][0][2 * h + q];
+                        const float tc = col == 0 ? tg.x : (col == 1 ? tg.y : tg.z);
+                        const float dd = y - tc, den = y * y + 0.01f;
+                        loss += dd * dd / den;
+                        d = 2.0f * dd / den * (inv_n / 3.0f);
+                    }
+                    dy[2 * h + q] = d;
+                }
+            }
+            ady[m][0][0] = pack_bf16(dy[0], dy[1]);
+            ady[m][0][1] = pack_bf16(dy[2], dy[3]);
+            ady[m][0][2] = 0u;
+            ady[m][0][3] = 0u;
+        }
+        store_frag_rows(gr.dz, base, n, kTGradStride / 2, kNrcHiddenLayers * kNrcHidden, ady, 1, g, t);
+        // backward: dH5 = dY W5, dZ5 = dH5 * [H5 > 0]
+        mlp_layer<16, 8>(swb + bwd_off(5), ady, acc, g, t);
+        mask_to_a(acc, gr.act, base, n, kNrcIn + 4 * kNrcHidden, a, g, t);
+        store_frag_rows(gr.dz, base, n, kTGradStride / 2, 4 * kNrcHidden, a, 4, g, t);
+#pragma unroll 1
+        for (int l = kNrcHiddenLayers - 1; l >= 1; --l) {  // dZ_l = (dZ_{l+1} W_l) * [H_l > 0]
+            mlp_layer<kNrcHidden, 8>(swb + bwd_off(l), a, acc, g, t);
+            mask_to_a(acc, gr.act, base, n, kNrcIn + (l - 1) * kNrcHidden, a, g, t);
+            store_frag_rows(gr.dz, base, n, kTGradStride / 2, (l - 1) * kNrcHidden, a, 4, g, t);
+        }
+        // encoding gradient dX = dZ1 W0 (32 columns), to lane = sample through shared memory
+        mlp_layer<kNrcHidden, 4>(swb + bwd_off(0), a, acc, g, t);
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    float* r = sx + (m * 16 + g + h * 8) * kXRow + nt * 8 + 2 * t;
+                    r[0] = acc[m][nt][2 * h];
+                    r[1] = acc[m][nt][2 * h + 1];
+                }
+        __syncwarp();
+        if (i < n) {
+            const float* dx = sx + lane * kXRow;
+#pragma unroll 1
+            for (int l = 0; l < kNrcLevels; ++l)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    uint32_t idx;
+                    float w;
+                    nrc_corner(v, l, p, c, idx, w);
+                    atomicAdd(reinterpret_cast<float2*>(gr.grid) + idx, make_float2(w * dx[2 * l], w * dx[2 * l + 1]));
+                }
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xFFFFFFFFu, loss, o);
+    if (lane == 0 && loss != 0.0f) atomicAdd(gr.loss, loss * inv_n / 3.0f);
+}
+
+GB_D void ldsm_x4_trans(uint32_t (&r)[4], const void* p) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
+constexpr int kWgTile = 64;              // samples per shared-memory tile
+constexpr int kWgRow = kNrcHidden + 8;   // padded BF16 row (144 B: ldmatrix rows hit distinct banks)
+
+// dW_l[o][k] += sum over the block's samples of dZ[m][o] H[m][k]; block =
+// (sample split, layer), 4 warps, warp w owns rows o in [16 w, 16 w + 16).
+__global__ void __launch_bounds__(128) nrc_wgrad_tc_kernel(const uint32_t* __restrict__ act,
+                                                          const uint32_t* __restrict__ dz, uint32_t n, uint32_t chunk,
+                                                          float* grad) {
+    const int l = blockIdx.y;
+    const int K = in_dim(l), O = out_dim(l), Opad = bwd_out_pad(l);
+    const int aoff = l == 0 ? 0 : kNrcIn + (l - 1) * kNrcHidden;     // BF16 column of H_l
+    const int doff = l == 5 ? kNrcHiddenLayers * kNrcHidden : l * kNrcHidden;  // BF16 column of dZ_{l+1}
+    __shared__ __align__(16) __nv_bfloat16 sa[kWgTile][kWgRow], sd[kWgTile][kWgRow];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const bool active = warp * 16 < Opad;
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+    const uint32_t m0 = blockIdx.x * chunk, m1 = min(n, m0 + chunk);
+    for (uint32_t mb = m0; mb < m1; mb += kWgTile) {
+        // stage 64 samples: H_l (K columns) and dZ (Opad columns), 16-byte pieces
+        for (int e = threadIdx.x; e < kWgTile * 8; e += blockDim.x) {
+            const int r = e >> 3, c8 = (e & 7) * 8;
+            const uint32_t m = mb + r;
+            uint4 va = make_uint4(0u, 0u, 0u, 0u), vd = va;
+            if (m < m1) {
+                if (c8 < K) va = *reinterpret_cast<const uint4*>(act + (size_t)m * (kTActStride / 2) + (aoff + c8) / 2);
+                if (c8 < Opad) vd = *reinterpret_cast<const uint4*>(dz + (size_t)m * (kTGradStride / 2) + (doff + c8) / 2);
+            }
+            *reinterpret_cast<uint4*>(&sa[r][c8]) = va;
+            *reinterpret_cast<uint4*>(&sd[r][c8]) = vd;
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll
+            for (int ks = 0; ks < kWgTile / 16; ++ks) {
+                // A = dZ^T (rows o, cols m): 8x8 blocks (m0, o0), (m0, o0+8), (m0+8, o0), (m0+8, o0+8)
+                const int mi = lane & 7, mat = lane >> 3;
+                uint32_t af[4];
+                ldsm_x4_trans(af, &sd[ks * 16 + (mat >> 1) * 8 + mi][warp * 16 + (mat & 1) * 8]);
+                const uint32_t afr[4] = {af[0], af[1], af[2], af[3]};
+#pragma unroll
+                for (int np = 0; np < 4; ++np) {
+                    if (np * 16 >= K) break;
+                    // B = H (rows m, cols k): blocks (m0, k0), (m0+8, k0), (m0, k0+8), (m0+8, k0+8)
+                    uint32_t bf[4];
+                    ldsm_x4_trans(bf, &sa[ks * 16 + (mat & 1) * 8 + mi][np * 16 + (mat >> 1) * 8]);
+                    mma_bf16(acc[2 * np], afr, bf[0], bf[1]);
+                    mma_bf16(acc[2 * np + 1], afr, bf[2], bf[3]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    float* gw = grad + f32_off(l);
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+        const int k = nt * 8 + 2 * t;
+        if (k >= K) break;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int o = warp * 16 + g + 8 * h;
+            if (o >= O) continue;
+            if (acc[nt][2 * h] != 0.0f) atomicAdd(gw + o * K + k, acc[nt][2 * h]);
+            if (acc[nt][2 * h + 1] != 0.0f) atomicAdd(gw + o * K + k + 1, acc[nt][2 * h + 1]);
+        }
+    }
+}
+
 struct AdamCfg {
     float lr, b1, b2, eps, c1, c2;  // c1 = 1 / (1 - b1^t), c2 = 1 / (1 - b2^t)
 };
@@ -610,8 +939,9 @@ struct gbrt_nrc {
     DevBuf mlp_w, mlp_h, mlp_g, mlp_m, mlp_v;
     DevBuf act, dz, loss, io_a, io_b;
     DevBuf mlp_tc, status;  // BF16 weights in tcgen05 core-matrix order; query status word
+    DevBuf mlp_bt;          // transposed BF16 weights of the tensor-core backward pass
     uint32_t step = 0;
-    int infer_blocks = 0, tc_blocks = 0;
+    int infer_blocks = 0, tc_blocks = 0, train_blocks = 0;
 };
 
 namespace {
@@ -641,12 +971,17 @@ cudaError_t nrc_refresh_copies(gbrt_nrc* r, cudaStream_t st) {
     nrc_copy_kernel<<<(n + 255) / 256, 256, 0, st>>>(r->grid_w.as<float>(), r->nentries, r->grid_h.as<__half2>(),
                                                      r->mlp_w.as<float>(), r->mlp_h.as<__nv_bfloat16>());
     nrc_tc_weights_kernel<<<(kTcWElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_tc.as<__nv_bfloat16>());
+    nrc_bwd_weights_kernel<<<(kBwdElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_bt.as<__nv_bfloat16>());
     return cudaGetLastError();
 }
 
+bool train_fp32(const gbrt_nrc* r) { return (r->cfg.flags & GBRT_NRC_TRAIN_FP32) != 0; }
+
 cudaError_t nrc_reserve_batch(gbrt_nrc* r, uint32_t n) {
-    cudaError_t e = r->act.reserve((size_t)n * kActStride * 4);
-    if (e == cudaSuccess) e = r->dz.reserve((size_t)n * kGradStride * 4);
+    const size_t a = train_fp32(r) ? (size_t)n * kActStride * 4 : (size_t)n * kTActStride * 2;
+    const size_t d = train_fp32(r) ? (size_t)n * kGradStride * 4 : (size_t)n * kTGradStride * 2;
+    cudaError_t e = r->act.reserve(a);
+    if (e == cudaSuccess) e = r->dz.reserve(d);
     return e;
 }
 
@@ -657,6 +992,17 @@ cudaError_t nrc_gradients(gbrt_nrc* r, const float4* pos, const float4* target, 
     if ((e = cudaMemsetAsync(r->grid_g.p, 0, r->grid_g.bytes, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(r->mlp_g.p, 0, r->mlp_g.bytes, st)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(r->loss.p, 0, 4, st)) != cudaSuccess) return e;
+    if (!train_fp32(r)) {
+        NrcTcGrad g{r->grid_g.as<float>(), r->loss.as<float>(), r->act.as<uint32_t>(), r->dz.as<uint32_t>()};
+        const uint32_t tiles = (n + 31) / 32;
+        const uint32_t blocks = std::min<uint32_t>((tiles + kTrainWarps - 1) / kTrainWarps, (uint32_t)r->train_blocks);
+        nrc_train_tc_kernel<<<blocks, kTrainWarps * 32, kTrainTcSmem, st>>>(
+            r->view, g, r->mlp_bt.as<__nv_bfloat16>(), pos, target, n, 1.0f / (float)n);
+        const uint32_t chunk = 2048, splits = (n + chunk - 1) / chunk;
+        nrc_wgrad_tc_kernel<<<dim3(splits, 6), 128, 0, st>>>(r->act.as<uint32_t>(), r->dz.as<uint32_t>(), n, chunk,
+                                                             r->mlp_g.as<float>());
+        return cudaGetLastError();
+    }
     NrcGrad g{r->grid_g.as<float>(), r->mlp_g.as<float>(), r->act.as<float>(), r->dz.as<float>(), r->loss.as<float>()};
     nrc_train_kernel<<<(n + 127) / 128, 128, kTrainSmem, st>>>(r->view, g, pos, target, n, 1.0f / (float)n);
     const uint32_t chunk = 1024, splits = (n + chunk - 1) / chunk;
@@ -682,6 +1028,7 @@ cudaError_t nrc_adam(gbrt_nrc* r, cudaStream_t st) {
                                                                      r->mlp_m.as<float>(), r->mlp_v.as<float>(), a,
                                                                      r->mlp_h.as<__nv_bfloat16>());
     nrc_tc_weights_kernel<<<(kTcWElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_tc.as<__nv_bfloat16>());
+    nrc_bwd_weights_kernel<<<(kBwdElems + 255) / 256, 256, 0, st>>>(r->mlp_w.as<float>(), r->mlp_bt.as<__nv_bfloat16>());
     return cudaGetLastError();
 }
 
@@ -698,11 +1045,16 @@ cudaError_t nrc_kernel_setup(gbrt_nrc* r) {
         if (e != cudaSuccess) return e;
         e = cudaFuncSetAttribute(nrc_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(nrc_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainTcSmem);
+        if (e != cudaSuccess) return e;
         int sms = 0, per = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, nrc_infer_kernel, 128, kInferSmem);
         r->infer_blocks = sms * std::max(per, 1);
+        int per_train = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_train, nrc_train_tc_kernel, kTrainWarps * 32, kTrainTcSmem);
+        r->train_blocks = sms * std::max(per_train, 1);
         e = cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
         if (e != cudaSuccess) return e;
         cudaFuncSetAttribute(nrc_infer_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -788,6 +1140,7 @@ int gbrt_nrc_create(gbrt_ctx* c, const gbrt_nrc_config* cfg, gbrt_nrc** out) {
         if (e == cudaSuccess) e = b->alloc(kNrcMlpParams * 4);
     if (e == cudaSuccess) e = r->mlp_h.alloc(kBf16Padded * 2);
     if (e == cudaSuccess) e = r->mlp_tc.alloc(kTcWElems * 2);
+    if (e == cudaSuccess) e = r->mlp_bt.alloc(kBwdElems * 2);
     if (e == cudaSuccess) e = r->status.alloc(4);
     if (e == cudaSuccess) e = r->loss.alloc(4);
     if (e != cudaSuccess) {

@@ -8,8 +8,10 @@ oracle shows that its path is ill-conditioned at the ulp level:
     tests, TIR, MASK/BLEND opacity, sky face), or
   * a secondary hit lay within TAU_EDGE of a triangle edge (margin[1]), or
   * the oracle's own sample leaves the 1e-4 band when its transcendentals
-    (sin, cos, pow, exp, log) are moved by 1 to 3 ulps (CUDA's and libm's
-    results differ by that much).
+    (sin, cos, pow, exp, log), dot products and normalised vectors are moved
+    by a few ulps (CUDA's and libm's transcendentals, and fused against
+    separate multiply-adds, differ by that much); each nudge size draws its
+    own signs, so several sizes are tried.
 The contract: no unexplained mismatch, and at most FLIP_MAX of the samples
 mismatched at all.
 """
@@ -23,7 +25,7 @@ FLIP_MAX = 2e-3
 # float ulps at 1.0.
 TAU_DECISION = 2.0 ** -14
 TAU_EDGE = 2.0 ** -14
-NUDGES = (1, 2, 3)
+NUDGES = (1, 2, 3, 4, 6, 8)
 
 
 def mismatched(a, b):

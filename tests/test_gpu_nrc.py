@@ -3,9 +3,14 @@
 * queries (FP16 table, BF16 tensor-core MLP with FP32 accumulation) agree
   with the float64 forward within 3% of the output scale, on tcgen05 (the
   default) and on mma.sync, and the two agree with each other within 1%;
-* the FP32 training pass gives the oracle's loss (1e-4 relative) and its
-  gradients: per layer and for the table, 1e-3 relative L2 error and every
-  entry within 1e-3 of the block's largest gradient;
+* the tensor-core training pass (BF16 operands, FP32 accumulation) gives
+  the loss and gradients of the oracle run with the same BF16 roundings
+  (1e-3 relative L2 per block), and stands no further from the exact
+  float64 gradients than that BF16 oracle does (the operand precision);
+* the FP32 training pass (GBRT_NRC_TRAIN_FP32) gives the oracle's loss
+  (1e-4 relative) and its gradients: per layer and for the table, 1e-3
+  relative L2 error and every entry within 1e-3 of the block's largest
+  gradient;
 * one Adam step from zero moments moves every parameter with a non-zero
   gradient by -lr * sign(g);
 * online training on a smooth target field lowers the loss 10x.
@@ -96,34 +101,73 @@ def test_tcgen05_follows_training(gpu_ctx):
     assert np.abs(ys[0] - ys[1]).max() <= 0.01 * scale
 
 
-def test_gradients_match_oracle(gpu_ctx):
-    rng = np.random.default_rng(4)
-    c = _cache(gpu_ctx)
-    mlp, grid = _random_params(rng)
-    c.set_params(mlp, grid)
-    pos = _points(rng, 3000)
-    tgt = rng.random((3000, 3)).astype(np.float32)
-    # drop samples sitting on a ReLU kink (a pre-activation within 1e-5 of
-    # its layer's scale): FP32 and float64 may take different sides there
+def _kink_free(mlp, grid, pos, bf16_ops):
+    """Samples whose pre-activations all sit away from the ReLU kink (1e-5
+    of the layer's scale): FP32 and float64 may take different sides there."""
     lv = N.level_table(BASE, GROWTH, LOG2T)
-    _, (_, _, hs, Ws) = N.forward(mlp, grid, _p01(pos), lv, LOG2T)
+    fwd = N.forward_bf16 if bf16_ops else N.forward
+    _, (_, _, hs, Ws) = fwd(mlp, grid, _p01(pos), lv, LOG2T)
     keep = np.ones(len(pos), bool)
     for l in range(5):
         z = np.abs(hs[l] @ Ws[l].T)
         keep &= z.min(axis=1) > 1e-5 * z.max(axis=1)
+    return keep
+
+
+def _grad_blocks(gm, gg, rgm, rgg):
+    bounds = [0, 2048, 6144, 10240, 14336, 18432, 18624]
+    blocks = [(gm[a:b], rgm[a:b], f"W{k}") for k, (a, b) in enumerate(zip(bounds[:-1], bounds[1:]))]
+    blocks.append((gg, rgg, "table"))
+    return {name: (np.linalg.norm(g - r) / np.linalg.norm(r), np.abs(g - r).max() / np.abs(r).max())
+            for g, r, name in blocks}
+
+
+def test_tc_gradients_match_oracle(gpu_ctx):
+    """Default training path: forward, backward and weight gradient on the
+    tensor cores (mma.sync, BF16 operands, FP32 accumulation)."""
+    rng = np.random.default_rng(14)
+    c = _cache(gpu_ctx)
+    mlp, grid = _random_params(rng)
+    c.set_params(mlp, grid)
+    pos = _points(rng, 5000)
+    tgt = rng.random((5000, 3)).astype(np.float32)
+    keep = _kink_free(mlp, grid, pos, True)
     assert keep.mean() > 0.9
     pos, tgt = pos[keep], tgt[keep]
     loss, gm, gg = c.train(pos, tgt, step=False, grads=True)
+    lv = N.level_table(BASE, GROWTH, LOG2T)
+    bl, bgm, bgg = N.loss_and_grads(mlp, grid, _p01(pos), tgt, lv, LOG2T, bf16_ops=True)
+    assert abs(loss - bl) <= 1e-4 * abs(bl)
+    errs = _grad_blocks(gm, gg, bgm, bgg)
+    assert all(rel < 1e-3 and worst < 1e-2 for rel, worst in errs.values()), errs
+    # against the exact float64 gradients: no further than the BF16-operand
+    # oracle itself (the precision BF16 operands give), plus the 1e-3 above
     rl, rgm, rgg = N.loss_and_grads(mlp, grid, _p01(pos), tgt, lv, LOG2T)
+    assert abs(loss - rl) <= 1e-2 * abs(rl)
+    errs = _grad_blocks(gm, gg, rgm, rgg)
+    prec = _grad_blocks(bgm, bgg, rgm, rgg)
+    assert all(errs[k][0] <= 1.1 * prec[k][0] + 1e-3 for k in errs), (errs, prec)
+    assert all(prec[k][0] < 0.1 for k in prec), prec
+
+
+def test_gradients_match_oracle(gpu_ctx):
+    from rustracer_gb300 import gbrt
+    rng = np.random.default_rng(4)
+    c = _cache(gpu_ctx, flags=gbrt.NRC_TRAIN_FP32)
+    mlp, grid = _random_params(rng)
+    c.set_params(mlp, grid)
+    pos = _points(rng, 3000)
+    tgt = rng.random((3000, 3)).astype(np.float32)
+    keep = _kink_free(mlp, grid, pos, False)
+    assert keep.mean() > 0.9
+    pos, tgt = pos[keep], tgt[keep]
+    loss, gm, gg = c.train(pos, tgt, step=False, grads=True)
+    rl, rgm, rgg = N.loss_and_grads(mlp, grid, _p01(pos), tgt, N.level_table(BASE, GROWTH, LOG2T), LOG2T)
     assert abs(loss - rl) <= 1e-4 * abs(rl)
     # per layer and for the table: relative L2 error 1e-3, every entry within
     # 1e-3 of that block's largest gradient (FP32 sums over 3000 samples in
     # atomic order against float64)
-    bounds = [0, 2048, 6144, 10240, 14336, 18432, 18624]
-    blocks = [(gm[a:b], rgm[a:b], f"W{k}") for k, (a, b) in enumerate(zip(bounds[:-1], bounds[1:]))]
-    blocks.append((gg, rgg, "table"))
-    errs = {name: (np.linalg.norm(g - r) / np.linalg.norm(r), np.abs(g - r).max() / np.abs(r).max())
-            for g, r, name in blocks}
+    errs = _grad_blocks(gm, gg, rgm, rgg)
     assert all(rel < 1e-3 and worst < 1e-3 for rel, worst in errs.values()), errs
 
 
