@@ -366,6 +366,10 @@ def run_batched(args):
     build.build()
     depth = DEPTH
     specs = [WL.batched_scene(i) for i in range(32)]
+    if args.mix == "small":  # the same scenes as small frames: 256^2 / 512^2 at 1-4 spp (seeded)
+        rng = np.random.default_rng(77)
+        specs = [(sd, int(r), int(r), int(rng.choice([1, 2, 4])))
+                 for (sd, _, _, _), r in zip(specs, rng.choice([256, 512], 32))]
     ctx = gbrt.Context(0)
     scs = [gbrt.Scene(ctx, sd) for sd, _, _, _ in specs]
     accs = [gbrt.Accum(ctx, w, h) for _, w, h, _ in specs]
@@ -376,7 +380,8 @@ def run_batched(args):
     tuned = [sc.autotune(sd.ubo(640, 360, samples=2, bounces=depth, exposure=1.0), 640, 360)
              for sc, (sd, _, _, _) in zip(scs, specs)]
     t_tune = time.perf_counter() - t_tune
-    ctx.jobs_configure(policy=gbrt.POLICY_SRPT | gbrt.JOB_LARGE_WAVES)  # throughput: waves up to 2^26 paths
+    # throughput: waves up to 2^26 paths (large frames); small frames keep the default 2^24 cap
+    ctx.jobs_configure(policy=gbrt.POLICY_SRPT | (gbrt.JOB_LARGE_WAVES if args.mix == "full" else 0))
 
     def batch():
         jobs = [ctx.submit(sc, u, a) for sc, u, a in zip(scs, ubos, accs)]
@@ -422,18 +427,22 @@ def run_batched(args):
             "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (32 seeded scenes of instanced tori, 1k-2M triangles per mesh)",
-            "config": {"workload": "batched32_instanced_alpha_transmissive", "scenes": 32,
+            "config": {"workload": "batched32_instanced_alpha_transmissive" + ("_small_frames" if args.mix == "small"
+                                                                                else ""), "scenes": 32,
                        "triangles_unique": int(sum(sd.num_triangles for sd, _, _, _ in specs)),
                        "instances": int(sum(len(sd.instances) for sd, _, _, _ in specs)),
                        "paths_per_step": int(px), "depth": depth,
-                       "resolutions": "{256^2, 512^2, 1280x720, 1920x1080}", "spp": "{1, 4, 16, 64}",
+                       "resolutions": "{256^2, 512^2}" if args.mix == "small" else "{256^2, 512^2, 1280x720, 1920x1080}",
+                       "spp": "{1, 2, 4}" if args.mix == "small" else "{1, 4, 16, 64}",
                        "l2": "inputs (1.2 GB of vertices) larger than L2", "timing": "host wall clock, submit to last image on host",
-                       "waves": "up to 2^26 paths (GBRT_JOB_LARGE_WAVES)"},
+                       "waves": "up to 2^26 paths (GBRT_JOB_LARGE_WAVES)" if args.mix == "full" else "up to 2^24 paths"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind, "kernel": "whole batch (algorithmic bytes)",
                          "bytes_per_ray_by_scene": [round(b, 1) for b in brays]},
             "sequential": {"value": seq_rays / seq_wall / 1e6, "unit": "Mrays/s",
+                           "ms_per_step": seq_wall / args.steps * 1e3,
                            "how": "the same 32 frames one after another through gbrt_render_ex"},
+            "batched_over_sequential": (rays / wall) / (seq_rays / seq_wall),
             "autotune": {"seconds": round(t_tune, 3),
                          "chosen_width": {str(w): sum(t["chosen_width"] == w for t in tuned) for w in (2, 4, 8)},
                          "sort_rays": sum(t["sort_rays"] for t in tuned),
@@ -497,6 +506,7 @@ def run_serving(args):
         t_end = time.perf_counter()
     clocks = clk.summary()
     lat = np.array([inf["latency_ms"] for inf in infos])
+    service = np.array([inf["latency_ms"] - inf["queue_ms"] for inf in infos])  # admitted (first wave) -> done
     cj = np.array([j["cache"] for j in trace], bool)
     rays = np.array([job_rays(inf)[0] for inf in infos], np.float64)
     shaded = np.array([job_rays(inf)[1] for inf in infos], np.float64)
@@ -523,6 +533,9 @@ def run_serving(args):
                            "p99_ms": float(np.percentile(lat[cj], 99)) if cj.any() else None,
                            "options": copts, "table": "16 x 2^19 x 2, one cache per scene"},
             "mean_queue_ms": float(np.mean([inf["queue_ms"] for inf in infos])),
+            "service_ms": {"p50": float(np.percentile(service, 50)), "p99": float(np.percentile(service, 99)),
+                           "how": "admission (the job's first wave) to image on the host"},
+            "queue_ms": {"p50": float(np.percentile(lat - service, 50)), "p99": float(np.percentile(lat - service, 99))},
             "throughput": {"value": value, "unit": "Mrays/s", "makespan_s": makespan,
                            "offered_load": float(makespan / max(trace[-1]["arrival"], 1e-9))},
             "roofline": {"bound": "hbm", "achieved": alg / makespan / 1e9, "peak": peak, "unit": "GB/s",
@@ -556,12 +569,28 @@ def run_nrc(args):
     else:
         tuning = {"chosen_width": int(args.tune[1]), "sort_rays": int(args.tune.endswith("s"))}
         sc.set_tuning(tuning["chosen_width"], bool(tuning["sort_rays"]))
-    ref_acc = gbrt.Accum(ctx, Wn, Hn)
-    chunk = 32
-    for k in range(0, args.ref_spp, chunk):
-        sc.render(sd.ubo(Wn, Hn, samples=chunk, total=k + chunk, bounces=depth, exposure=1.0, has_sky=True), ref_acc,
-                  image=False, mode=MODES["wavefront"])
-    ref = ref_acc.download()[..., :3] / float(args.ref_spp)
+    if args.judge == "cpu64":
+        # the oracle with FP64 intersection and accumulation on every host core, over
+        # samples disjoint from the GPU runs' (global indices from 2^24 up)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        acc64 = np.zeros((Hn * Wn, 4), np.float32)
+        t0 = time.time()
+        off = 1 << 24
+        ref_st = O.OracleScene(sd).render(sd.ubo(Wn, Hn, samples=args.ref_spp, total=off + args.ref_spp,
+                                                 bounces=depth, exposure=1.0, has_sky=True), Wn, Hn,
+                                          accum=acc64, fp64=True, out=False)["stats"]
+        ref = acc64.reshape(Hn, Wn, 4)[..., :3] / float(args.ref_spp)
+        judge = {"kind": "FP64-intersection CPU oracle", "spp": args.ref_spp, "seconds": round(time.time() - t0, 1),
+                 "threads": int(ref_st["threads"]), "samples": f"global indices {off}..{off + args.ref_spp - 1}"}
+    else:
+        ref_acc = gbrt.Accum(ctx, Wn, Hn)
+        chunk = 32
+        for k in range(0, args.ref_spp, chunk):
+            sc.render(sd.ubo(Wn, Hn, samples=chunk, total=k + chunk, bounces=depth, exposure=1.0, has_sky=True),
+                      ref_acc, image=False, mode=MODES["wavefront"])
+        ref = ref_acc.download()[..., :3] / float(args.ref_spp)
+        judge = {"kind": "FP32 GPU path tracing (wavefront)", "spp": args.ref_spp}
     den = ref * ref + 1e-2
 
     def relmse(acc, spp):
@@ -595,11 +624,17 @@ def run_nrc(args):
     cache = gbrt.Nrc(ctx, tuple(map(float, lo)), tuple(map(float, hi)), log2_table=19, learning_rate=1e-3)
     losses = []
 
+    cache_mode = gbrt.NRC_MODE_PRIMARY_INDIRECT if args.nrc_mode == "primary" else gbrt.NRC_MODE_SUFFIX
+    frames = [0]
+
     def nrc_step(acc, spp):
+        # the first --nrc-warmup frames are plain path tracing that trains the cache (disabled = 1)
         k = args.nrc_spp
+        warm = frames[0] < args.nrc_warmup
+        frames[0] += 1
         r = cache.render(sc, sd.ubo(Wn, Hn, samples=k, total=spp + k, bounces=depth, exposure=1.0, has_sky=True),
                          acc, image=False, min_roughness=args.nrc_min_roughness, train_samples=args.nrc_samples,
-                         train_steps=args.nrc_steps)
+                         train_steps=args.nrc_steps, disabled=warm, mode=cache_mode)
         losses.append(r["loss"])
         return float(r["stats"]["device_ms"]), int(r["stats"]["rays_total"]), k
 
@@ -614,12 +649,12 @@ def run_nrc(args):
             "data": "synthetic (seeded city block of instanced boxes and spheres)",
             "config": {"workload": f"city_nrc_{Wn}x{Hn}_depth{depth}", "instances": int(len(sd.instances)),
                        "instanced_triangles": int(sd.instanced_triangles), "point_lights": 16, "sky": True,
-                       "reference": f"{args.ref_spp} spp wavefront path tracing (FP32; an FP64 CPU reference at "
-                                    f"this size does not fit the run)",
+                       "reference": judge,
                        "cache": {"levels": 16, "table": 1 << 19, "features": 2, "mlp": "32-64x5-3 ReLU",
                                  "spp_per_frame": args.nrc_spp, "train_samples_per_frame": args.nrc_samples,
                                  "adam_steps_per_frame": args.nrc_steps, "lr": 1e-3,
-                                 "min_roughness": args.nrc_min_roughness},
+                                 "min_roughness": args.nrc_min_roughness, "mode": args.nrc_mode,
+                                 "warmup_frames": args.nrc_warmup},
                        "tuning": {"chosen_width": tuning["chosen_width"], "sort_rays": tuning["sort_rays"]}},
             "plain_pt": {"time_s": None if t_pt is None else t_pt / 1e3, "curve": pts_pt[:: max(1, len(pts_pt) // 24)],
                          "mrays_per_s": rays_pt / tot_pt / 1e3},
@@ -677,13 +712,24 @@ def main():
                     help="icosphere: the headline frame; batched: 32 scenes as one batch of jobs; "
                          "serving: Poisson job arrivals with p50/p99 latency")
     ap.add_argument("--jobs", type=int, default=200, help="serving: jobs in the trace")
+    ap.add_argument("--mix", default="full", choices=["full", "small"],
+                    help="batched: the configuration's resolutions and spp (full), or small frames (256^2/512^2 "
+                         "at 1-4 spp) of the same scenes")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--ref-spp", type=int, default=1024, help="nrc: samples of the reference image")
+    ap.add_argument("--judge", default="gpu32", choices=["gpu32", "cpu64"],
+                    help="nrc: reference image from FP32 GPU path tracing, or from the FP64-intersection CPU "
+                         "oracle (use with a small --res, e.g. 240x136)")
     ap.add_argument("--max-frames", type=int, default=200, help="nrc: frame limit of the plain run (x4 for the cache)")
     ap.add_argument("--nrc-min-roughness", type=float, default=0.25, help="nrc: roughness a cache vertex needs")
     ap.add_argument("--nrc-spp", type=int, default=4, help="nrc: samples per cache frame")
     ap.add_argument("--nrc-samples", type=int, default=1 << 16, help="nrc: training samples per frame")
     ap.add_argument("--nrc-steps", type=int, default=1, help="nrc: Adam steps per frame")
+    ap.add_argument("--nrc-mode", default="suffix", choices=["suffix", "primary"],
+                    help="nrc: cache vertex = first rough hit after the camera hit (suffix), or the camera hit "
+                         "itself for its indirect light (primary)")
+    ap.add_argument("--nrc-warmup", type=int, default=0,
+                    help="nrc: frames of plain path tracing that train the cache before it is used")
     args = ap.parse_args()
     global W, H, SPP, WORKLOAD
     if args.res:

@@ -650,22 +650,34 @@ int gbrt_nrc_query_device(gbrt_nrc* nrc, const float* pos4_dev, uint32_t n, floa
 int gbrt_nrc_train(gbrt_nrc* nrc, const float* pos4, const float* target4, uint32_t n, int step, float* loss,
                    float* grad_mlp, float* grad_grid);
 
-/* A frame rendered with the cache (wavefront form).  A path's cache vertex
- * is its first hit after the camera hit whose material roughness factor
- * (1 - glossiness for specular-glossiness) is >= min_roughness.  Render
- * paths stop there and add throughput x cache(position); about
- * train_samples paths per frame (chosen by a hash of pixel and sample) trace
- * on as plain path tracing and give one training sample each: the radiance
- * gathered from their cache vertex on, divided by the throughput reaching
- * it.  After the frame, train_steps Adam steps on those samples; *loss (may
- * be NULL) gets the loss of the last step.  disabled = 1: no path stops (the image is
- * plain path tracing; the cache still trains). */
+/* A frame rendered with the cache (wavefront form).  About train_samples
+ * paths per frame (chosen by a hash of pixel and sample) trace on as plain
+ * path tracing and give one training sample each; after the frame,
+ * train_steps Adam steps on those samples; *loss (may be NULL) gets the loss
+ * of the last step.  disabled = 1: no path stops (the image is plain path
+ * tracing; the cache still trains).  Modes:
+ *  - GBRT_NRC_MODE_SUFFIX (0): a path's cache vertex is its first hit after
+ *    the camera hit whose material roughness factor (1 - glossiness for
+ *    specular-glossiness) is >= min_roughness.  Render paths stop there and
+ *    add throughput x cache(position); a training sample is the radiance
+ *    gathered from the cache vertex on, divided by the throughput reaching it.
+ *  - GBRT_NRC_MODE_PRIMARY_INDIRECT (1): the cache vertex is the camera hit
+ *    (roughness >= min_roughness).  Render paths shade it as usual (emission,
+ *    next-event estimation) and then stop, adding cache(position) for all the
+ *    radiance that would have come after it; a training sample is the
+ *    radiance a full path gathers after the camera hit's own emission and
+ *    next-event estimation (zero when the path ends there).  The camera sees
+ *    each point from one direction, so the position-only cache represents the
+ *    view-dependent indirect light of glossy surfaces for a fixed camera. */
 typedef struct gbrt_nrc_render_opts {
     float min_roughness;
     uint32_t train_samples;
     uint32_t train_steps;
     uint32_t disabled;
+    uint32_t mode;  /* GBRT_NRC_MODE_* */
 } gbrt_nrc_render_opts;
+#define GBRT_NRC_MODE_SUFFIX 0u
+#define GBRT_NRC_MODE_PRIMARY_INDIRECT 1u
 int gbrt_render_nrc(gbrt_scene* scene, gbrt_nrc* nrc, const gbrt_ubo* ubo, gbrt_accum* accum, uint8_t* out_rgba8,
                     gbrt_stats* stats, const gbrt_nrc_render_opts* opts, float* loss);
 

@@ -31,7 +31,7 @@ static_assert(sizeof(gbrt_skin_raw) == 16384, "Skin is 256 mat4");
 static_assert(sizeof(gbrt_ray) == 32 && sizeof(gbrt_hit) == 24, "ray/hit records");
 static_assert(sizeof(gbrt_stats) == 104, "stats record");
 static_assert(sizeof(gbrt_job_info) == 128 && sizeof(gbrt_job_desc) == 64, "job records");
-static_assert(sizeof(gbrt_nrc_config) == 56 && sizeof(gbrt_nrc_render_opts) == 16, "cache records");
+static_assert(sizeof(gbrt_nrc_config) == 56 && sizeof(gbrt_nrc_render_opts) == 20, "cache records");
 static_assert(sizeof(gbrt_tune_report) == 40, "tune report");
 static_assert(sizeof(gbrt_scene_info) == 40, "scene info");
 

@@ -115,6 +115,8 @@ struct NrcWave {
     uint32_t train_thresh;
     float min_roughness;
     uint32_t disabled;  // 1: no path stops at the cache (plain path tracing plus training samples)
+    uint32_t mode;      // GBRT_NRC_MODE_*: 0 the cache vertex is the first rough hit after the camera hit;
+                        // 1 (primary indirect) the camera hit, whose indirect radiance the cache returns
 };
 
 // CUDA-event pairs around every wavefront launch, grouped by stage

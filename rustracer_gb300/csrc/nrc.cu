@@ -998,7 +998,8 @@ cudaError_t nrc_gradients(gbrt_nrc* r, const float4* pos, const float4* target, 
         const uint32_t blocks = std::min<uint32_t>((tiles + kTrainWarps - 1) / kTrainWarps, (uint32_t)r->train_blocks);
         nrc_train_tc_kernel<<<blocks, kTrainWarps * 32, kTrainTcSmem, st>>>(
             r->view, g, r->mlp_bt.as<__nv_bfloat16>(), pos, target, n, 1.0f / (float)n);
-        const uint32_t chunk = 2048, splits = (n + chunk - 1) / chunk;
+        // 512-sample chunks: 768 blocks for a 2^16 batch, about 5 per SM
+        const uint32_t chunk = 512, splits = (n + chunk - 1) / chunk;
         nrc_wgrad_tc_kernel<<<dim3(splits, 6), 128, 0, st>>>(r->act.as<uint32_t>(), r->dz.as<uint32_t>(), n, chunk,
                                                              r->mlp_g.as<float>());
         return cudaGetLastError();
@@ -1302,6 +1303,7 @@ cudaError_t nrc_frame(gbrt_nrc* r, const DevScene& view, const gbrt_ubo& ubo, co
     nw.train_thresh = (uint32_t)std::min(65536.0, std::ceil(frac * 65536.0));
     nw.min_roughness = opts.min_roughness;
     nw.disabled = opts.disabled ? 1u : 0u;
+    nw.mode = opts.mode;
     WfState w = wf;
     w.cap = cap;
     *what = "wavefront launch";
@@ -1348,6 +1350,7 @@ extern "C" int gbrt_render_nrc(gbrt_scene* s, gbrt_nrc* r, const gbrt_ubo* ubo, 
     if (ubo->number_of_samples == 0 || ubo->total_number_of_samples < ubo->number_of_samples)
         return fail(c, GBRT_E_INVALID, "need 0 < number_of_samples <= total_number_of_samples");
     if (ubo->number_of_bounces > 31) return fail(c, GBRT_E_INVALID, "the wavefront form handles at most 31 bounces");
+    if (opts->mode > GBRT_NRC_MODE_PRIMARY_INDIRECT) return fail(c, GBRT_E_INVALID, "unknown radiance-cache mode");
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
     const uint32_t W = acc->w, H = acc->h, ns = ubo->number_of_samples;

@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(256) wf_nrc_apply(WfState st, NrcWave nrc, uin
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 L = nrc.qout[i];
         const uint32_t pid = __float_as_uint(L.w) & kPidMask;
-        const float4 tp = st.tp[pid], r = st.rad[pid];
+        // primary-indirect mode: the cache returns the camera hit's indirect radiance itself
+        const float4 tp = nrc.mode == 1u ? f4(1.0f, 1.0f, 1.0f, 0.0f) : st.tp[pid], r = st.rad[pid];
         st.rad[pid] = f4(r.x + tp.x * fmaxf(L.x, 0.0f), r.y + tp.y * fmaxf(L.y, 0.0f), r.z + tp.z * fmaxf(L.z, 0.0f),
                          r.w);
     }
@@ -246,7 +247,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 else if (feat == 0u) wf_shade<0u><<<g_grid.shade_plain, kShadeThreads, 0, stream>>>(w, st, b);
                 else wf_shade<kFeatAll><<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b);
                 te();
-                if (nrc && b >= 1 && !nrc->disabled) {  // cache queries of the paths that stopped here
+                if (nrc && !nrc->disabled && (nrc->mode == 1u ? b == 0 : b >= 1)) {  // queries of the paths that stopped here
                     tb(3);
                     if ((e = gbrt_host::nrc_query_counted(cache, nrc->query, nrc->counts + b, J.npaths, nrc->qout,
                                                           stream)) != cudaSuccess)

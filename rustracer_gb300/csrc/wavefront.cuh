@@ -292,9 +292,29 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             Rp.rngState = make_uint4(P.x, P.y, rg.z, rg.y);
             const uint32_t inst = __float_as_uint(h4.w);
             bool cached = false;  // a render path stopping at the radiance cache
+            bool stop_after = false;  // primary-indirect mode: shade this camera hit, then stop at the cache
             if constexpr (kNrc) {
                 const bool train = nrc_train_hash(P.pix, P.sg->sample0 + P.j) < nrc->train_thresh;
-                if (b >= 1u && inst != 0xFFFFFFFFu && (train || !nrc->disabled) &&
+                if (nrc->mode == 1u) {
+                    // camera hit: render paths take the cache's indirect radiance after shading it;
+                    // training paths mark the vertex (w = 2) and record the radiance gathered so far
+                    // at the next bounce (after this vertex's emission and shadow-tested NEE)
+                    if (b == 0u && inst != 0xFFFFFFFFu && hit_roughness(s, inst) >= nrc->min_roughness) {
+                        const float3 o = f3(st.ray_o[0][R + q]);
+                        const float3 x = f3(fmaf(h4.x, d.x, o.x), fmaf(h4.x, d.y, o.y), fmaf(h4.x, d.z, o.z));
+                        if (train) {
+                            nrc->snap_pos[pid] = f4(x, 2.0f);
+                            nrc->snap_tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);
+                        } else if (!nrc->disabled) {
+                            stop_after = true;
+                            const uint32_t k = atomicAdd(&nrc->counts[0], 1u);
+                            nrc->query[k] = f4(x, __uint_as_float(word));
+                        }
+                    } else if (b == 1u && train && nrc->snap_pos[pid].w == 2.0f) {
+                        nrc->snap_pos[pid].w = 1.0f;
+                        nrc->snap_rad[pid] = rad4;
+                    }
+                } else if (b >= 1u && inst != 0xFFFFFFFFu && (train || !nrc->disabled) &&
                     hit_roughness(s, inst) >= nrc->min_roughness) {
                     const float3 o = f3(st.ray_o[b & 1][R + q]);
                     const float3 x = f3(fmaf(h4.x, d.x, o.x), fmaf(h4.x, d.y, o.y), fmaf(h4.x, d.z, o.z));
@@ -348,6 +368,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 tp *= Rp.hitValue;
                 if (!Rp.needScatter || Rp.t < 0.0f) cont = false;
             }
+            if (stop_after) cont = false;
             st.tp[pid] = f4(tp, Rp.t);
             st.rad[pid] = f4(rad, Rp.volume_dis);
             st.hp[pid] = f4(Rp.hitPoint, __uint_as_float(Rp.RandomSeed));
@@ -443,13 +464,14 @@ GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave*
         if constexpr (kNrc) {  // training sample: suffix radiance / throughput at the vertex
             const float4 sp = nrc->snap_pos[pid];
             if (sp.w != 0.0f) {
-                const float3 r0 = f3(nrc->snap_rad[pid]), t0 = f3(nrc->snap_tp[pid]);
+                // w = 2: a marked camera hit whose path ended there: no indirect radiance
+                const float3 r0 = sp.w == 2.0f ? r : f3(nrc->snap_rad[pid]), t0 = f3(nrc->snap_tp[pid]);
                 const float3 dr = r - r0;
                 const float3 tg = f3(t0.x > 0.0f ? dr.x / t0.x : 0.0f, t0.y > 0.0f ? dr.y / t0.y : 0.0f,
                                      t0.z > 0.0f ? dr.z / t0.z : 0.0f);
                 const uint32_t k = atomicAdd(&nrc->counts[32], 1u);
                 if (k < nrc->train_max) {
-                    nrc->train_pos[k] = sp;
+                    nrc->train_pos[k] = f4(f3(sp), 1.0f);
                     nrc->train_tgt[k] = f4(tg, 0.0f);
                 }
             }

@@ -164,11 +164,11 @@ class Context:
         self.check(self.L.gbrt_jobs_inject(self.h, kind, count))
 
     def submit(self, scene, ubo, accum, image=True, skins=None, cache=None, min_roughness=0.0,
-               train_samples=1 << 16, train_steps=1):
+               train_samples=1 << 16, train_steps=1, cache_mode=0):
         """Queues one frame of `scene` into `accum` (through the radiance
         cache `cache`, an Nrc, when given); returns a Job."""
         return Job(self, scene, ubo, accum, image, skins, cache,
-                   None if cache is None else NrcRenderOpts(min_roughness, train_samples, train_steps, 0))
+                   None if cache is None else NrcRenderOpts(min_roughness, train_samples, train_steps, 0, cache_mode))
 
     def close(self):
         if getattr(self, "h", None):
@@ -234,11 +234,13 @@ class NrcConfig(C.Structure):
 
 NRC_QUERY_MMA_SYNC = 0x1
 NRC_TRAIN_FP32 = 0x2
+NRC_MODE_SUFFIX = 0
+NRC_MODE_PRIMARY_INDIRECT = 1
 
 
 class NrcRenderOpts(C.Structure):
     _fields_ = [("min_roughness", C.c_float), ("train_samples", C.c_uint32), ("train_steps", C.c_uint32),
-                ("disabled", C.c_uint32)]
+                ("disabled", C.c_uint32), ("mode", C.c_uint32)]
 
 
 class Nrc:
@@ -294,13 +296,13 @@ class Nrc:
         return (float(loss[0]), gm, gg) if grads else float(loss[0])
 
     def render(self, scene, ubo, accum, image=True, min_roughness=0.0, train_samples=1 << 16, train_steps=1,
-               disabled=False):
+               disabled=False, mode=NRC_MODE_SUFFIX):
         """One frame with the cache (gbrt_render_nrc); returns dict(image, stats, loss)."""
         ubo = np.asarray(ubo, T.UBO).reshape(())
         img = np.zeros((accum.h_, accum.w, 4), np.uint8) if image else None
         st = np.zeros((), T.STATS)
         loss = np.zeros(1, np.float32)
-        opts = NrcRenderOpts(min_roughness, train_samples, train_steps, int(disabled))
+        opts = NrcRenderOpts(min_roughness, train_samples, train_steps, int(disabled), mode)
         self.ctx.check(self.ctx.L.gbrt_render_nrc(scene.h, self.h, _p(ubo), accum.h, _p(img) if image else None,
                                                   _p(st), C.byref(opts), _p(loss)))
         return dict(image=img, stats=st, loss=float(loss[0]))

@@ -40,7 +40,7 @@ def test_struct_sizes():
     assert T.VERTEX.itemsize == 128 and T.MATERIAL.itemsize == 256 and T.UBO.itemsize == 324
     assert T.LIGHT.itemsize == 48 and T.INSTANCE.itemsize == 64 and T.PRIMINFO.itemsize == 16
     assert T.JOB_INFO.itemsize == 128 and C.sizeof(gbrt.JobDesc) == 64
-    assert C.sizeof(gbrt.NrcConfig) == 56 and C.sizeof(gbrt.NrcRenderOpts) == 16
+    assert C.sizeof(gbrt.NrcConfig) == 56 and C.sizeof(gbrt.NrcRenderOpts) == 20
 
 
 def test_no_device_is_an_error_not_a_crash():
