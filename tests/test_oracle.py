@@ -317,3 +317,25 @@ def test_float_skybox_bilinear_texels():
     assert np.array_equal(sky((0.5, 1.0, -0.5)), np.float32([20, 2, 0]))
     assert np.array_equal(sky((-0.5, 1.0, 0.5)), np.float32([30, 3, 0]))
     assert np.allclose(sky((0.0, 1.0, 0.0)), [25.0, 2.5, 0.0], rtol=1e-6)
+
+
+def test_city_fp32_and_fp64_intersection_agree():
+    """The radiance-cache workload's judge: on the city block (4,001
+    flattened instances, sky, 16 lights) the oracle's FP32 render and its
+    FP64-intersection, FP64-accumulation render of the same samples differ by
+    a relMSE far below the 1e-2 convergence target, so a reference of N
+    samples path traced in FP32 (the GPU matches the FP32 oracle sample by
+    sample) stands for the FP64 reference of those samples."""
+    from rustracer_gb300 import workloads as WL
+    sd = WL.city_scene()
+    o = O.OracleScene(sd)
+    W, H, N = 48, 28, 16
+    imgs = []
+    for fp64 in (False, True):
+        acc = np.zeros((H * W, 4), np.float32)
+        o.render(sd.ubo(W, H, samples=N, total=N, bounces=12, exposure=1.0, has_sky=True), W, H, accum=acc,
+                 fp64=fp64, out=False)
+        imgs.append(acc.reshape(H, W, 4)[..., :3] / N)
+    assert imgs[0].mean() > 0.05
+    relmse = float(np.mean((imgs[0] - imgs[1]) ** 2 / (imgs[1] ** 2 + 1e-2)))
+    assert relmse < 1e-4, relmse
