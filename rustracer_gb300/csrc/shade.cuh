@@ -178,24 +178,13 @@ GB_D float3 rotate_point(float4 q, float3 v) {  // :373-376
     const float3 a = f3(q.x, q.y, q.z);
     return 2.0f * dot(a, v) * a + (q.w * q.w - dot(a, a)) * v + 2.0f * q.w * cross(a, v);
 }
-GB_D float3 sample_hemisphere(float2 u) {  // :381-394
-    float a = sqrtf(u.x);
-    float b = GB_TWO_PI * u.y;
-    float sb, cb;
-    sincosf(b, &sb, &cb);
-    return f3(a * cb, a * sb, sqrtf(1.0f - u.x));
-}
-GB_D float3 sample_ggx_vndf(float3 Ve, float alpha, float2 u) {  // sampleGGXVNDF, :413-436
+// sampleGGXVNDF, :413-436, given the polar sample t1 = sqrt(u.x) cos(2 pi u.y),
+// t2 = sqrt(u.x) sin(2 pi u.y) (eval_indirect draws it once for both lobes).
+GB_D float3 sample_ggx_vndf_polar(float3 Ve, float alpha, float t1, float t2) {
     float3 Vh = normalize3(f3(alpha * Ve.x, alpha * Ve.y, Ve.z));
     float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
     float3 T1 = lensq > 0.0f ? f3(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : f3(1.0f, 0.0f, 0.0f);
     float3 T2 = cross(Vh, T1);
-    float r = sqrtf(u.x);
-    float phi = GB_TWO_PI * u.y;
-    float sp, cp;
-    sincosf(phi, &sp, &cp);
-    float t1 = r * cp;
-    float t2 = r * sp;
     float s = 0.5f * (1.0f + Vh.z);
     t2 = mixf(sqrtf(1.0f - t1 * t1), t2, s);
     float3 Nh = t1 * T1 + t2 * T2 + sqrtf(fmaxf(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;
@@ -253,21 +242,32 @@ GB_D bool eval_indirect(float2 u, float3 N, float3 Ng, float3 V, const MatBrdf& 
     float3 Vl = rotate_point(q, V);
     const float3 Nl = f3(0.0f, 0.0f, 1.0f);
     float3 Ll = f3(0.0f);
-    if (type == DIFFUSE_TYPE) {
-        Ll = sample_hemisphere(u);
-        const BrdfData d = prepare_brdf(Nl, Ll, Vl, m);
-        weight = (1.0f - m.specular_factor * d.F) * d.diffuseReflectance * frostbite_diffuse(d);
-        weight *= (1.0f - m.transmission);
-    } else if (type == SPECULAR_TYPE) {
-        const BrdfData d = prepare_brdf(Nl, f3(0.0f, 0.0f, 1.0f), Vl, m);
-        float3 Hl = d.alpha == 0.0f ? f3(0.0f, 0.0f, 1.0f) : sample_ggx_vndf(Vl, d.alpha, u);
-        Ll = reflect3(-Vl, Hl);
-        float HdotL = fmaxf(0.00001f, fminf(1.0f, dot(Hl, Ll)));
-        float NdotL = fmaxf(0.00001f, fminf(1.0f, Ll.z));
-        float NdotV = fmaxf(0.00001f, fminf(1.0f, Vl.z));
-        float3 F = fresnel(d.specularF0, shadowed_f90(m.F90), HdotL);
-        weight = F * g2_over_g1(d.alphaSquared, NdotL, NdotV);
-        weight *= m.specular_factor;
+    if (type == DIFFUSE_TYPE || type == SPECULAR_TYPE) {
+        // Both lobes start from the same polar sample of u (sampleHemisphere :381-394 and
+        // sampleGGXVNDF :413-436 both take sqrt(u.x) and the angle 2 pi u.y) and from
+        // prepareBRDFData, at the sampled direction for the diffuse lobe and at the normal for
+        // the specular one; computing those once keeps the lanes of a warp together whichever
+        // lobe each path chose.
+        const bool diffuse = type == DIFFUSE_TYPE;
+        const float ru = sqrtf(u.x);
+        float su, cu;
+        sincosf(GB_TWO_PI * u.y, &su, &cu);
+        const float t1 = ru * cu, t2 = ru * su;
+        if (diffuse) Ll = f3(t1, t2, sqrtf(1.0f - u.x));
+        const BrdfData d = prepare_brdf(Nl, diffuse ? Ll : Nl, Vl, m);
+        if (diffuse) {
+            weight = (1.0f - m.specular_factor * d.F) * d.diffuseReflectance * frostbite_diffuse(d);
+            weight *= (1.0f - m.transmission);
+        } else {  // sampleSpecularMicrofacet, :587-616
+            float3 Hl = d.alpha == 0.0f ? f3(0.0f, 0.0f, 1.0f) : sample_ggx_vndf_polar(Vl, d.alpha, t1, t2);
+            Ll = reflect3(-Vl, Hl);
+            float HdotL = fmaxf(0.00001f, fminf(1.0f, dot(Hl, Ll)));
+            float NdotL = fmaxf(0.00001f, fminf(1.0f, Ll.z));
+            float NdotV = fmaxf(0.00001f, fminf(1.0f, Vl.z));
+            float3 F = fresnel(d.specularF0, shadowed_f90(m.F90), HdotL);
+            weight = F * g2_over_g1(d.alphaSquared, NdotL, NdotV);
+            weight *= m.specular_factor;
+        }
     } else if (type == TRANSMISSION_TYPE) {
         if (m.volume) {
             const float eta = m.frontFace ? 1.0f / m.ior : m.ior;
