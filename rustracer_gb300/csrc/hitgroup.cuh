@@ -115,11 +115,12 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     const float4 uv1 = f4(__ldg(&v1->uv0[0]), __ldg(&v1->uv0[1]), __ldg(&v1->uv1[0]), __ldg(&v1->uv1[1]));
     const float4 uv2 = f4(__ldg(&v2->uv0[0]), __ldg(&v2->uv0[1]), __ldg(&v2->uv1[0]), __ldg(&v2->uv1[1]));
     const float4 uv01 = uv0 * b0 + uv1 * b1 + uv2 * b2;
-    const float3 p0 = ldg3(v0->pos), p1 = ldg3(v1->pos), p2 = ldg3(v2->pos);
+    // pos and normal are the first two 16-byte fields of the 128-byte vertex: one vector load each
+    const float3 p0 = f3(ldg4(v0->pos)), p1 = f3(ldg4(v1->pos)), p2 = f3(ldg4(v2->pos));
     const float3 pos = p0 * b0 + p1 * b1 + p2 * b2;
     const float4 col = ldg4(v0->color) * b0 + ldg4(v1->color) * b1 + ldg4(v2->color) * b2;
-    float3 normal = normalize3(normalize3(ldg3(v0->normal)) * b0 + normalize3(ldg3(v1->normal)) * b1 +
-                               normalize3(ldg3(v2->normal)) * b2);
+    float3 normal = normalize3(normalize3(f3(ldg4(v0->normal))) * b0 + normalize3(f3(ldg4(v1->normal))) * b1 +
+                               normalize3(f3(ldg4(v2->normal))) * b2);
     const float4 tangent = normalize4(ldg4(v0->tangent) * b0 + ldg4(v1->tangent) * b1 + ldg4(v2->tangent) * b2);
     float3 Ng = normal_xform(T, cross(p1 - p0, p2 - p0));
     float3 origin = point_xform(T, pos);

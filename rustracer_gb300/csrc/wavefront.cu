@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(128, trace_minb(kMode))
 // without textures, specular-glossiness or debug shading, whose smaller body
 // runs at more resident blocks).
 template <uint32_t kFeat>
-__global__ void __launch_bounds__(kShadeThreads, kFeat ? kShadeMinBlocks : kShadePlainMinBlocks)
+__global__ void __launch_bounds__(kFeat ? kShadeThreads : kShadePlainThreads,
+                                  kFeat ? kShadeMinBlocks : kShadePlainMinBlocks)
     wf_shade(const __grid_constant__ SingleWave w, WfState st, uint32_t b) {
     shade_body<SingleWave, false, kFeat>(w, st, b);
 }
@@ -118,7 +119,7 @@ cudaError_t grids(Grid& g) {
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, wf_shade<kFeatAll>, kShadeThreads, 0)) != cudaSuccess)
         return e;
     int bp = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp, wf_shade<0u>, kShadeThreads, 0)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp, wf_shade<0u>, kShadePlainThreads, 0)) != cudaSuccess)
         return e;
     g.shade_plain = sms * (bp > 0 ? bp : 1);
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bh, wf_shadow<kTraceWide>, 128, 0)) != cudaSuccess) return e;
@@ -244,7 +245,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                 if (side && b > 0 && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
                 tb(1);
                 if (nrc) wf_shade_nrc<<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b, *nrc);
-                else if (feat == 0u) wf_shade<0u><<<g_grid.shade_plain, kShadeThreads, 0, stream>>>(w, st, b);
+                else if (feat == 0u) wf_shade<0u><<<g_grid.shade_plain, kShadePlainThreads, 0, stream>>>(w, st, b);
                 else wf_shade<kFeatAll><<<g_grid.shade, kShadeThreads, 0, stream>>>(w, st, b);
                 te();
                 if (nrc && !nrc->disabled && (nrc->mode == 1u ? b == 0 : b >= 1)) {  // queries of the paths that stopped here
@@ -262,7 +263,11 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                     if ((e = cudaStreamWaitEvent(side->stream, side->shaded, 0)) != cudaSuccess) return e;
                     ss = side->stream;
                 }
+#ifdef GBRT_SHADOW_BINARY  // experiment: shadow rays through the binary BVH whatever the extension rays use
+                if (mode == kTraceWide) wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+#else
                 if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+#endif
                 else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
                 else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
                 if (side && (e = cudaEventRecord(side->shadowed, ss)) != cudaSuccess) return e;

@@ -48,12 +48,21 @@ namespace gbrt {
 #ifndef GBRT_SHADE_MINB
 #define GBRT_SHADE_MINB 2
 #endif
+// The form without textures, specular-glossiness and debug shading fits 80
+// registers: 2 blocks of 384 threads (24 warps per SM).  Icosphere frame,
+// threads x blocks: 128 x 6 4627, 192 x 4 4656, 256 x 3 4609, 384 x 2 4689
+// Mrays/s (larger blocks make longer octant-grouped runs of rays and the
+// barrier of the grouped append waits on fewer partial blocks).
+#ifndef GBRT_SHADE_PLAIN_THREADS
+#define GBRT_SHADE_PLAIN_THREADS 384
+#endif
 #ifndef GBRT_SHADE_PLAIN_MINB
-#define GBRT_SHADE_PLAIN_MINB 3
+#define GBRT_SHADE_PLAIN_MINB 2
 #endif
 constexpr int kShadeThreads = GBRT_SHADE_THREADS;  // block size of the shade kernels
 constexpr int kShadeMinBlocks = GBRT_SHADE_MINB;   // resident blocks per SM the shade kernels are compiled for
-// ... and the form without textures, specular-glossiness and debug shading
+// ... and of the form without textures, specular-glossiness and debug shading
+constexpr int kShadePlainThreads = GBRT_SHADE_PLAIN_THREADS;
 constexpr int kShadePlainMinBlocks = GBRT_SHADE_PLAIN_MINB;
 
 GB_D uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -191,16 +200,20 @@ GB_D void extend_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
     const float4* __restrict__ ro = st.ray_o[b & 1] + R;
     const float4* __restrict__ rd = st.ray_d[b & 1] + R;
     TraceStats ts{0, 0, 0};
+    // the any-hit context (pixel and sample of a BLEND draw) is only read when an alpha test can run
+    const bool alpha = !(J.flags & GBRT_RAY_OPAQUE) && !J.s.all_opaque;
     world_trace<false, kMode>(
         J.s, n, &cnt[kWorkExt + b], J.flags, ts,
         [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
             const float4 o4 = ro[q], d4 = rd[q];
-            const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
             o = f3(o4);
             d = f3(d4);
             tmin = 0.001f;
             tmax = J.tfar;
-            ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b};
+            if (alpha) {
+                const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
+                ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b};
+            }
         },
         [&](uint32_t q, bool hit, const Hit& h) {
             st.hit[R + q] = f4(hit ? h.t : -1.0f, h.u, h.v, __uint_as_float(hit ? h.inst : 0xFFFFFFFFu));
@@ -413,16 +426,19 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
     const float4* __restrict__ sd = st.sh_d + R;
     TraceStats ts{0, 0, 0};
     const uint32_t flags = GBRT_RAY_TERMINATE_ON_FIRST | J.flags;
+    const bool alpha = !(J.flags & GBRT_RAY_OPAQUE) && !J.s.all_opaque;
     world_trace<true, kMode>(
         J.s, n, &cnt[kWorkSh + b], flags, ts,
         [&](uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx) {
             const float4 o4 = so[q], d4 = sd[q];
-            const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
             o = f3(o4);
             d = f3(d4);
             tmin = 0.1f;
             tmax = o4.w;
-            ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b | 0x100u};
+            if (alpha) {
+                const PathXY P = decode_path(w, __float_as_uint(d4.w), J.out.width);
+                ctx = AnyCtx{P.x, P.y, P.sg->sample0 + P.j, b | 0x100u};
+            }
         },
         [&](uint32_t q, bool occluded, const Hit&) {
             const float4 d4 = sd[q], e4 = st.sh_e[R + q], c4 = st.sh_c[R + q];
