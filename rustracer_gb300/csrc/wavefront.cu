@@ -263,11 +263,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                     if ((e = cudaStreamWaitEvent(side->stream, side->shaded, 0)) != cudaSuccess) return e;
                     ss = side->stream;
                 }
-#ifdef GBRT_SHADOW_BINARY  // experiment: shadow rays through the binary BVH whatever the extension rays use
-                if (mode == kTraceWide) wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
-#else
                 if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
-#endif
                 else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
                 else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
                 if (side && (e = cudaEventRecord(side->shadowed, ss)) != cudaSuccess) return e;
