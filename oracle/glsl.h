@@ -20,9 +20,10 @@
 namespace glsl {
 
 // Parity diagnostics (the ORC_DIAG build of the oracle only): every dot
-// product and normalised vector passes through diag_round, which moves it by
-// a few ulps in nudge mode -- the size of the differences that fused
-// multiply-adds make on the GPU.  Without ORC_DIAG it is the identity.
+// product, length, refraction root and normalised vector passes through
+// diag_round, which moves it by a few ulps in nudge mode -- the size of the
+// differences that fused multiply-adds and approximate square roots make on
+// the GPU.  Without ORC_DIAG it is the identity.
 #ifdef ORC_DIAG
 float diag_round(float r);
 #else
@@ -101,7 +102,7 @@ inline vec3 cross(vec3 a, vec3 b) {
     return vec3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 inline float inversesqrt(float x) { return 1.0f / std::sqrt(x); }
-inline float length(vec3 a) { return std::sqrt(dot(a, a)); }
+inline float length(vec3 a) { return diag_round(std::sqrt(dot(a, a))); }
 inline vec3 normalize(vec3 a) {
     const vec3 r = a * inversesqrt(dot(a, a));
     return vec3(diag_round(r.x), diag_round(r.y), diag_round(r.z));
@@ -121,7 +122,7 @@ inline vec3 refract(vec3 I, vec3 N, float eta) {
     float d = dot(N, I);
     float k = 1.0f - eta * eta * (1.0f - d * d);
     if (k < 0.0f) return vec3(0.0f);
-    return eta * I - (eta * d + std::sqrt(k)) * N;
+    return eta * I - (eta * d + diag_round(std::sqrt(k))) * N;
 }
 
 // ---- vec4 ----

@@ -53,7 +53,8 @@ namespace {
 // A GPU sample can leave the 1e-4 band around the oracle's sample when its
 // path meets a decision whose operands sit so close to the threshold that
 // ulp-level differences in the arithmetic before it (CUDA's sin/cos/pow/exp/
-// log against libm's, fused multiply-adds) take the other side, or when the
+// log against libm's, approximate divisions and square roots, fused
+// multiply-adds) take the other side, or when the
 // path amplifies those ulps continuously (a GGX lobe evaluated near its peak
 // cancels 1 - NdotH^2).  Per sample the oracle records:
 //  - margin[0]: the smallest |operand - threshold| of the decisions taken:
@@ -72,7 +73,8 @@ namespace {
 // a barycentric, all of unit scale, so the margins are absolute.  Decisions
 // between integer-exact quantities (the uniform light pick) come out the same
 // on both sides and are not logged.  In nudge mode every transcendental
-// result, dot product and normalised vector component is moved by +-k ulps
+// result, shading division and square root, dot product, length and
+// normalised vector component is moved by +-k ulps
 // (sign drawn from a per-sample counter hash): samples that then leave the
 // 1e-4 band are ill-conditioned at the ulp level.
 // ---------------------------------------------------------------------------
@@ -109,8 +111,15 @@ inline float t_sin(float a) { return nudged(std::sin(a)); }
 inline float t_cos(float a) { return nudged(std::cos(a)); }
 inline vec3 t_exp(vec3 a) { return vec3(nudged(std::exp(a.x)), nudged(std::exp(a.y)), nudged(std::exp(a.z))); }
 inline vec3 t_log(vec3 a) { return vec3(nudged(std::log(a.x)), nudged(std::log(a.y)), nudged(std::log(a.z))); }
-// Seed of a sample's nudge signs (mixed with the nudge size, so each size
-// draws other signs).
+// The shaders' divisions and square roots, nudged in diagnostics mode like the
+// transcendentals: the CUDA shading kernels compute them in approximate forms
+// (within 2 ulps).
+inline float dv(float a, float b) { return nudged(a / b); }
+inline vec3 dv(vec3 a, float b) { return vec3(dv(a.x, b), dv(a.y, b), dv(a.z, b)); }
+inline float sq(float a) { return nudged(std::sqrt(a)); }
+// Seed of a sample's nudge signs (mixed with the nudge argument: its size in
+// the low 16 bits, a draw index above them, so each size and draw has its
+// own signs).
 inline uint32_t nudge_seed(uint32_t x, uint32_t y, uint32_t s) { return (x * 73856093u) ^ (y * 19349663u) ^ (s * 83492791u) ^ 0x5bd1e995u; }
 
 // ---------------------------------------------------------------------------
@@ -232,13 +241,13 @@ struct MaterialBrdf {
 };
 
 float Schlick(const float cosine, const float refractionIndex) {  // PBR.glsl:48-53
-    float r0 = (1.0f - refractionIndex) / (1.0f + refractionIndex);
+    float r0 = dv(1.0f - refractionIndex, 1.0f + refractionIndex);
     r0 *= r0;
     return r0 + (1.0f - r0) * t_pow(1.0f - cosine, 5.0f);
 }
 
 void matBuild(MaterialBrdf& m) {  // PBR.glsl:195-206
-    float factor = (m.ior - OURSIDE_IOR) / (m.ior + OURSIDE_IOR);
+    float factor = dv(m.ior - OURSIDE_IOR, m.ior + OURSIDE_IOR);
     m.dielectricSpecularF0 = min(factor * factor * m.specular_color_factor, vec3(1.0f)) * m.specular_factor;
     m.dielectricSpecularF90 = m.specular_color_factor;
     m.F0 = mix(m.dielectricSpecularF0, m.baseColor, m.metallic);
@@ -254,24 +263,24 @@ vec3 evalFresnel(vec3 f0, float f90, float NdotS) {  // PBR.glsl:228-243
 }
 
 float Smith_G_a(float alpha, float NdotS) {  // PBR.glsl:248-250
-    return NdotS / (std::max(0.00001f, alpha) * std::sqrt(1.0f - std::min(0.99999f, NdotS * NdotS)));
+    return dv(NdotS, std::max(0.00001f, alpha) * sq(1.0f - std::min(0.99999f, NdotS * NdotS)));
 }
 float Smith_G_Lambda_GGX(float a) {  // PBR.glsl:253-255
-    return (-1.0f + std::sqrt(1.0f + (1.0f / (a * a)))) * 0.5f;
+    return (-1.0f + sq(1.0f + dv(1.0f, a * a))) * 0.5f;
 }
 float Smith_G2_Height_Correlated(float alpha, float NdotL, float NdotV) {  // :258-262
     float aL = Smith_G_a(alpha, NdotL);
     float aV = Smith_G_a(alpha, NdotV);
-    return 1.0f / (1.0f + Smith_G_Lambda_GGX(aL) + Smith_G_Lambda_GGX(aV));
+    return dv(1.0f, 1.0f + Smith_G_Lambda_GGX(aL) + Smith_G_Lambda_GGX(aV));
 }
 float GGX_D(float alphaSquared, float NdotH) {  // PBR.glsl:286-289
     float b = ((alphaSquared - 1.0f) * NdotH * NdotH + 1.0f);
-    return alphaSquared / (PI * b * b);
+    return dv(alphaSquared, PI * b * b);
 }
 vec3 evalMicrofacet(const BrdfData& d) {  // PBR.glsl:292-303
     float D = GGX_D(std::max(0.00001f, d.alphaSquared), d.NdotH);
     float G2 = Smith_G2_Height_Correlated(d.alpha, d.NdotL, d.NdotV);
-    return ((d.F * G2 * D) / (4.0f * d.NdotL * d.NdotV)) * d.NdotL;
+    return dv(d.F * G2 * D, 4.0f * d.NdotL * d.NdotV) * d.NdotL;
 }
 float shadowedF90(const vec3 F90) { return std::min(1.0f, luminance(F90)); }  // :312-322
 
@@ -286,14 +295,14 @@ BRDFProb getBrdfProbability(const MaterialBrdf& mat, vec3 V, vec3 shadingNormal)
     float diffuse = penetration * (1.0f - mat.transmission);
     float transmission = penetration * mat.transmission;
     float sum = std::max(0.0001f, (specular + diffuse + transmission));
-    float p = specular / sum;
+    float p = dv(specular, sum);
     p = clamp(p, 0.001f, 0.9f);
     float d = (1.0f - p) * (1.0f - mat.transmission);
     float t = (1.0f - p) * mat.transmission;
     sum = p + d + t;
-    p /= sum;
-    d /= sum;
-    t /= sum;
+    p = dv(p, sum);
+    d = dv(d, sum);
+    t = dv(t, sum);
     return {p, d, t};
 }
 
@@ -310,35 +319,35 @@ vec3 rotatePoint(vec4 q, vec3 v) {  // PBR.glsl:373-376
 vec4 invertRotation(vec4 q) { return vec4(-q.x, -q.y, -q.z, q.w); }  // PBR.glsl:580-583
 
 vec3 sampleHemisphere(vec2 u) {  // PBR.glsl:381-394
-    float a = std::sqrt(u.x);
+    float a = sq(u.x);
     float b = TWO_PI * u.y;
-    return vec3(a * t_cos(b), a * t_sin(b), std::sqrt(1.0f - u.x));
+    return vec3(a * t_cos(b), a * t_sin(b), sq(1.0f - u.x));
 }
 
 vec3 sampleGGXVNDF(vec3 Ve, vec2 alpha2D, vec2 u) {  // PBR.glsl:413-436
     vec3 Vh = normalize(vec3(alpha2D.x * Ve.x, alpha2D.y * Ve.y, Ve.z));
     float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
-    vec3 T1 = lensq > 0.0f ? vec3(-Vh.y, Vh.x, 0.0f) * inversesqrt(lensq) : vec3(1.0f, 0.0f, 0.0f);
+    vec3 T1 = lensq > 0.0f ? vec3(-Vh.y, Vh.x, 0.0f) * nudged(inversesqrt(lensq)) : vec3(1.0f, 0.0f, 0.0f);
     vec3 T2 = cross(Vh, T1);
-    float r = std::sqrt(u.x);
+    float r = sq(u.x);
     float phi = TWO_PI * u.y;
     float t1 = r * t_cos(phi);
     float t2 = r * t_sin(phi);
     float s = 0.5f * (1.0f + Vh.z);
-    t2 = mix(std::sqrt(1.0f - t1 * t1), t2, s);
-    vec3 Nh = t1 * T1 + t2 * T2 + std::sqrt(std::max(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;
+    t2 = mix(sq(1.0f - t1 * t1), t2, s);
+    vec3 Nh = t1 * T1 + t2 * T2 + sq(std::max(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;
     return normalize(vec3(alpha2D.x * Nh.x, alpha2D.y * Nh.y, std::max(0.0f, Nh.z)));
 }
 
 float Smith_G1_GGX(float alpha, float NdotS, float alphaSquared, float NdotSSquared) {  // :446-448
     (void)alpha;
     (void)NdotS;
-    return 2.0f / (std::sqrt(((alphaSquared * (1.0f - NdotSSquared)) + NdotSSquared) / NdotSSquared) + 1.0f);
+    return dv(2.0f, sq(dv((alphaSquared * (1.0f - NdotSSquared)) + NdotSSquared, NdotSSquared)) + 1.0f);
 }
 float Smith_G2_Over_G1_Height_Correlated(float alpha, float alphaSquared, float NdotL, float NdotV) {  // :470-474
     float G1V = Smith_G1_GGX(alpha, NdotV, alphaSquared, NdotV * NdotV);
     float G1L = Smith_G1_GGX(alpha, NdotL, alphaSquared, NdotL * NdotL);
-    return G1L / (G1V + G1L - G1V * G1L);
+    return dv(G1L, G1V + G1L - G1V * G1L);
 }
 float frostbiteDisneyDiffuse(const BrdfData& d) {  // PBR.glsl:486-496
     float energyBias = 0.5f * d.roughness;
@@ -419,7 +428,7 @@ bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, v
         sampleWeight *= material.specular_factor;
     } else if (brdfType == TRANSMISSION_TYPE) {
         if (material.volume) {
-            const float refraction_ratio = material.frontFace ? 1.0f / material.ior : material.ior;
+            const float refraction_ratio = material.frontFace ? dv(1.0f, material.ior) : material.ior;
             const float dn = dot(Nlocal, -Vlocal);
             note_margin(1.0f - refraction_ratio * refraction_ratio * (1.0f - dn * dn));  // refract's k
             const vec3 refracted = refract(-Vlocal, Nlocal, refraction_ratio);
@@ -436,7 +445,7 @@ bool evalIndirectCombinedBRDF(vec2 u, vec3 shadingNormal, vec3 geometryNormal, v
         if (!material.frontFace && material.volume) {
             float dis = volume_dis;
             volume_dis = -1.0f;
-            vec3 sigma = t_log(material.attenuation_color) / material.attenuation_distance;
+            vec3 sigma = dv(t_log(material.attenuation_color), material.attenuation_distance);
             vec3 attenuation = t_exp(sigma * dis);
             sampleWeight *= min(attenuation, vec3(1.0f));
         }
@@ -462,17 +471,17 @@ vec3 evalCombinedBRDF(vec3 N, vec3 L, vec3 V, const MaterialBrdf& material) {  /
 constexpr uint32_t SPECULAR_GLOSS_WORKFLOW = 1;
 constexpr float c_MinRoughness = 0.04f;
 float convertMetallic(vec3 diffuse, vec3 specular, float maxSpecular) {  // Material.glsl:78-89
-    float perceivedDiffuse = std::sqrt(0.299f * diffuse.x * diffuse.x + 0.587f * diffuse.y * diffuse.y +
+    float perceivedDiffuse = sq(0.299f * diffuse.x * diffuse.x + 0.587f * diffuse.y * diffuse.y +
                                        0.114f * diffuse.z * diffuse.z);
-    float perceivedSpecular = std::sqrt(0.299f * specular.x * specular.x + 0.587f * specular.y * specular.y +
+    float perceivedSpecular = sq(0.299f * specular.x * specular.x + 0.587f * specular.y * specular.y +
                                         0.114f * specular.z * specular.z);
     if (perceivedSpecular < c_MinRoughness) return 0.0f;
     float a = c_MinRoughness;
-    float b = perceivedDiffuse * (1.0f - maxSpecular) / (1.0f - c_MinRoughness) + perceivedSpecular -
+    float b = dv(perceivedDiffuse * (1.0f - maxSpecular), 1.0f - c_MinRoughness) + perceivedSpecular -
               2.0f * c_MinRoughness;
     float c = c_MinRoughness - perceivedSpecular;
     float D = std::max(b * b - 4.0f * a * c, 0.0f);
-    return clamp((-b + std::sqrt(D)) / (2.0f * a), 0.0f, 1.0f);
+    return clamp(dv(-b + sq(D), 2.0f * a), 0.0f, 1.0f);
 }
 
 constexpr uint32_t POINT_LIGHT = 1;
@@ -483,7 +492,7 @@ vec3 getLightIntensityAtPoint(const gbrt_light_raw& light, float distance) {  //
         const float radiusSquared = radius * radius;
         const float distanceSquared = distance * distance;
         const float attenuation =
-            2.0f / (distanceSquared + radiusSquared + distance * std::sqrt(distanceSquared + radiusSquared));
+            dv(2.0f, distanceSquared + radiusSquared + distance * sq(distanceSquared + radiusSquared));
         return color * attenuation;
     }
     return color;
@@ -1144,8 +1153,8 @@ vec3 sample_sky(const orc_scene& s, vec3 d) {
         ma = az;
         if (d.z >= 0.0f) { face = 4; sc = d.x; tc = -d.y; } else { face = 5; sc = -d.x; tc = -d.y; }
     }
-    float su = 0.5f * (sc / ma + 1.0f);
-    float sv = 0.5f * (tc / ma + 1.0f);
+    float su = 0.5f * (dv(sc, ma) + 1.0f);
+    float sv = 0.5f * (dv(tc, ma) + 1.0f);
     return sample_bilinear(s.sky_faces[face], vec2(su, sv)).xyz();
 }
 
@@ -1252,15 +1261,16 @@ bool sampleLightRIS(const orc_scene& s, uvec4& rngState, vec3 hitPosition, vec3 
             const float candidateRISWeight = candidatePdfG * candidateWeight;
             totalWeights += candidateRISWeight;
             const float accept = rand(rngState);
-            note_margin(accept - candidateRISWeight / totalWeights);
-            if (accept < (candidateRISWeight / totalWeights)) {
+            const float acceptRatio = dv(candidateRISWeight, totalWeights);
+            note_margin(accept - acceptRatio);
+            if (accept < acceptRatio) {
                 selectedSample = candidate;
                 samplePdfG = candidatePdfG;
             }
         }
     }
     if (totalWeights == 0.0f) return false;
-    lightSampleWeight = (totalWeights / float(3)) / samplePdfG;
+    lightSampleWeight = dv(dv(totalWeights, float(3)), samplePdfG);
     return true;
 }
 
@@ -1456,7 +1466,7 @@ void closest_hit(FrameCtx& f, RayPayload& Ray, const HitT& hit, const float* wdi
     if (ubo.debug == 1) {  // rchit:437-474 (legacy; D5)
         vec3 wd = vec3(wdir[0], wdir[1], wdir[2]);
         if (matbrdf.transmission > 0.0f) {
-            const float refraction_ratio = frontFace ? 1.0f / ior : ior;
+            const float refraction_ratio = frontFace ? dv(1.0f, ior) : ior;
             const float cos_theta = std::fabs(cos);
             const vec3 refracted = refract(wd, outwardNormal, refraction_ratio);
             const float reflectProb = refracted != vec3(0.0f) ? Schlick(cos_theta, refraction_ratio) : 1.0f;
@@ -1880,7 +1890,8 @@ int orc_render_diag(orc_scene* s, const gbrt_ubo* ubo, uint32_t W, uint32_t H, u
             float last_t = 0.0f;
             for (uint32_t si = 0; si < ns; ++si) {
                 gbrt_hit* ph = primary_hits ? &primary_hits[pix * ns + si] : nullptr;
-                SampleDiag diag{{INFINITY, INFINITY}, nudge_ulps, nudge_seed(x, y, sbase + si) ^ (nudge_ulps * 0x9E3779B9u)};
+                SampleDiag diag{{INFINITY, INFINITY}, nudge_ulps & 0xFFFFu,
+                                nudge_seed(x, y, sbase + si) ^ (nudge_ulps * 0x9E3779B9u)};
 #ifdef ORC_DIAG
                 g_diag = (sample_margins || nudge_ulps) ? &diag : nullptr;
 #endif

@@ -68,9 +68,11 @@ int  orc_render(orc_scene* s, const gbrt_ubo* ubo, uint32_t width, uint32_t heig
  * [pixel][sample][2] floats: [0] the smallest |operand - threshold| of the
  * branch decisions the sample's path took, [1] the smallest barycentric of
  * its secondary hits (both +inf when none).  nudge_ulps > 0 moves every
- * transcendental result (sin, cos, pow, exp, log) by that many ulps, up or
- * down by a per-sample hash, to expose samples that ulp-level arithmetic
- * differences change. */
+ * transcendental result (sin, cos, pow, exp, log), shading division and
+ * square root, dot product, length and normalised vector component by
+ * (nudge_ulps & 0xFFFF) ulps, up or down by a hash of the sample and of the
+ * whole nudge_ulps value (the bits above 16 select another draw of signs), to
+ * expose samples that ulp-level arithmetic differences change. */
 int  orc_render_diag(orc_scene* s, const gbrt_ubo* ubo, uint32_t width, uint32_t height,
                      uint32_t row0, uint32_t row1, float* accum, uint8_t* out_rgba8,
                      float* sample_radiance, gbrt_hit* primary_hits, float* sample_margins,

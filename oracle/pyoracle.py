@@ -143,12 +143,15 @@ class OracleScene:
         return hits, st
 
     def render(self, ubo, width, height, rows=None, accum=None, want_samples=False, want_hits=False,
-               fp64=False, threads=0, out=True, want_margins=False, nudge_ulps=0):
+               fp64=False, threads=0, out=True, want_margins=False, nudge_ulps=0, nudge_draw=0):
         """Renders rows [row0, row1) (all by default).  want_margins adds
         'margins' [pixel][sample][2] (smallest branch-decision margin,
         smallest secondary-hit barycentric); nudge_ulps > 0 moves every
-        transcendental by that many ulps (orc_render_diag)."""
+        transcendental, shading division and square root, dot product and
+        normalised vector by that many ulps with signs of draw `nudge_draw`
+        (orc_render_diag)."""
         from rustracer_gb300 import types as T
+        assert 0 <= nudge_ulps < 1 << 16 and 0 <= nudge_draw < 1 << 16
         ns = int(ubo["number_of_samples"])
         row0, row1 = rows if rows is not None else (0, height)
         img = np.zeros((height, width, 4), np.uint8) if out else None
@@ -158,7 +161,8 @@ class OracleScene:
         st = np.zeros((), STATS)
         ubo = np.ascontiguousarray(ubo)
         rc = self.L.orc_render_diag(self.h, _p(ubo), width, height, row0, row1, _p(accum), _p(img), _p(samples),
-                                   _p(hits), _p(margins), int(nudge_ulps), int(fp64), threads, _p(st))
+                                   _p(hits), _p(margins), int(nudge_ulps) | (int(nudge_draw) << 16), int(fp64),
+                                   threads, _p(st))
         assert rc == 0, rc
         return dict(image=img, samples=samples, hits=hits, stats=st, margins=margins)
 

@@ -19,6 +19,14 @@ LIB = os.path.join(HERE, "libgbrt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler",
                      "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-warn-spills"]
+# Path-tracing translation units: their plain `/` and sqrtf feed shading only
+# (BRDF terms, pdfs, normalisations), so they compile to the approximate
+# forms.  Every result that must match the CPU bit for bit -- camera rays, ray
+# setup, the triangle test, texture filtering on the any-hit path -- is written
+# with the explicit IEEE intrinsics (__fdiv_rn, __fsqrt_rn), which these flags
+# do not touch.
+SHADING_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
+SHADING_UNITS = {"wavefront.cu", "wave_multi.cu", "render.cu"}
 
 
 def nvcc():
@@ -55,7 +63,8 @@ def build(force=False, verbose=False, ptxas_info=False):
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [nv] + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
+        unit = SHADING_FLAGS if os.path.basename(src) in SHADING_UNITS else []
+        cmd = [nv] + NVCC_FLAGS + unit + extra + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -7,11 +7,15 @@ oracle shows that its path is ill-conditioned at the ulp level:
     (oracle margin[0]: Russian roulette, lobe choice, RIS acceptance, facing
     tests, TIR, MASK/BLEND opacity, sky face), or
   * a secondary hit lay within TAU_EDGE of a triangle edge (margin[1]), or
-  * the oracle's own sample leaves the 1e-4 band when its transcendentals
-    (sin, cos, pow, exp, log), dot products and normalised vectors are moved
-    by a few ulps (CUDA's and libm's transcendentals, and fused against
-    separate multiply-adds, differ by that much); each nudge size draws its
-    own signs, so several sizes are tried.
+  * the oracle's own sample moves by more than 1e-4 (relative, with no
+    absolute floor: a dark sample whose path changes under the nudges is as
+    ill-conditioned as a bright one) when its transcendentals (sin, cos, pow,
+    exp, log), shading divisions and square roots, dot products, lengths and
+    normalised vectors are moved by a few ulps (CUDA's and libm's
+    transcendentals, the shading kernels' approximate divisions and square
+    roots, and fused against separate multiply-adds differ by that much);
+    each nudge size and draw has its own signs, so several of each are
+    tried (the oracle re-renders only the rows that hold candidates).
 The contract: no unexplained mismatch, and at most FLIP_MAX of the samples
 mismatched at all.
 """
@@ -26,11 +30,12 @@ FLIP_MAX = 2e-3
 TAU_DECISION = 2.0 ** -14
 TAU_EDGE = 2.0 ** -14
 NUDGES = (1, 2, 3, 4, 6, 8)
+NUDGE_DRAWS = 3
 
 
-def mismatched(a, b):
+def mismatched(a, b, abs_tol=ABS_TOL):
     a, b = a.reshape(-1, 3).astype(np.float64), b.reshape(-1, 3).astype(np.float64)
-    return ~np.all(np.abs(a - b) <= REL_TOL * np.maximum(np.abs(a), np.abs(b)) + ABS_TOL, axis=1)
+    return ~np.all(np.abs(a - b) <= REL_TOL * np.maximum(np.abs(a), np.abs(b)) + abs_tol, axis=1)
 
 
 def classify(gpu, ref, oracle, ubo, width, height, rows=None):
@@ -50,10 +55,15 @@ def classify(gpu, ref, oracle, ubo, width, height, rows=None):
     bad = mismatched(g, o)
     near = (m[:, 0] < TAU_DECISION) | (m[:, 1] < TAU_EDGE)
     sens = np.zeros_like(bad)
-    if np.any(bad & ~near):
+    cand = np.nonzero(bad & ~near)[0]
+    per_row = width * ns
+    for row in np.unique(cand // per_row) + r0:
+        sel = cand[cand // per_row == row - r0]
         for k in NUDGES:
-            nb = oracle.render(ubo, width, height, rows=(r0, r1), want_samples=True, out=False, nudge_ulps=k)
-            sens |= mismatched(band(nb["samples"], 3), o)
+            for draw in range(NUDGE_DRAWS):
+                nb = oracle.render(ubo, width, height, rows=(int(row), int(row) + 1), want_samples=True, out=False,
+                                   nudge_ulps=k, nudge_draw=draw)
+                sens[sel] |= mismatched(band(nb["samples"], 3)[sel], o[sel], abs_tol=0.0)
     explained = bad & (near | sens)
     return dict(n=len(g), mismatched=int(bad.sum()), explained=int(explained.sum()),
                 by_margin=int((bad & near).sum()), by_nudge=int((bad & ~near & sens).sum()),

@@ -3,8 +3,9 @@ oracle's diagnostics build that it relies on.
 
 * The diagnostics build renders the plain build's bits when no diagnostic
   is asked for, and its margins are finite where paths made decisions.
-* Nudging transcendentals and dot products by ulps leaves most samples in
-  the 1e-4 band: the contract's "explained" class is small.
+* Nudging transcendentals, shading divisions and square roots and dot
+  products by ulps leaves most samples within 1e-4 (relative, no absolute
+  floor, as the contract tests them): the "explained" class is small.
 * A planted mistake -- the oracle re-rendered with every material's
   roughness off by 1%, standing in for a shading bug -- produces
   unexplained mismatches, so the contract does not explain real errors
@@ -44,7 +45,7 @@ def test_nudged_oracle_mostly_in_band(ico):
     sd, ubo, orc, ref = ico
     for k in parity.NUDGES:
         nb = orc.render(ubo, 48, 32, want_samples=True, nudge_ulps=k)
-        moved = parity.mismatched(nb["samples"], ref["samples"])
+        moved = parity.mismatched(nb["samples"], ref["samples"], abs_tol=0.0)
         assert moved.mean() < 0.01, (k, moved.mean())
     c = parity.classify(ref["samples"], ref, orc, ubo, 48, 32)
     assert c["mismatched"] == 0 and c["unexplained"] == 0
