@@ -46,6 +46,7 @@ GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32
     uint32_t q = 0;
     TRay r;
     Hit best;
+    float best_det = 1.0f;  // any-hit queries: best.u, best.v hold V, W of the world hit until the ray is done
     AnyCtx ctx{0, 0, 0, 0};
     float tmin = 0.0f, tmax = 0.0f;
     int cur = kEmpty, sp = 0;
@@ -65,6 +66,7 @@ GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32
                         load(q, o, d, tmin, tmax, ctx);
                         best.t = tmax;
                         best.u = best.v = 0.0f;
+                        best_det = 1.0f;
                         best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
                         iter = 0;
                         if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
@@ -148,16 +150,26 @@ GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32
                 const TriRec* tr = s.tris + first + i;
                 const float4 pa = __ldg(&tr->a), pb = __ldg(&tr->b), pc = __ldg(&tr->c);
                 ts.tris++;
-                float t, u, v;
-                if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                // any-hit queries keep V, W and det of the hit and divide once the ray is done (if
+                // their caller reads u, v at all); closest-hit queries divide per accepted hit
+                float t, u, v, det = 1.0f;
+                if constexpr (kAny) {
+                    if (!isect_tri_t(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v, det)) continue;
+                } else {
+                    if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                }
                 const uint32_t inst = __float_as_uint(pa.w);
                 const uint32_t prim = __float_as_uint(pb.w);
                 const uint32_t gw = __float_as_uint(pc.w);
                 if (!closer(t, inst, prim, best)) continue;
-                if (test_alpha && !(gw >> 31) && anyhit_ignore(s, s.inst[inst].custom, prim, inst, u, v, ctx)) continue;
+                if (test_alpha && !(gw >> 31) &&
+                    anyhit_ignore(s, s.inst[inst].custom, prim, inst, kAny ? __fdiv_rn(u, det) : u,
+                                  kAny ? __fdiv_rn(v, det) : v, ctx))
+                    continue;
                 best.t = t;
                 best.u = u;
                 best.v = v;
+                best_det = det;
                 best.inst = inst;
                 best.prim = prim;
                 best.bgeo = gw & 0x7FFFFFFFu;
@@ -169,6 +181,10 @@ GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32
         }
         if (!done && cur == kEmpty) done = true;
         if (done) {
+            if constexpr (kAny) {
+                best.u = __fdiv_rn(best.u, best_det);
+                best.v = __fdiv_rn(best.v, best_det);
+            }
             if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu)) {
                 // transformed instances: finish the ray with the two-level pass
                 trace_tlas<kAny>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);
@@ -211,6 +227,7 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
     uint32_t q = 0, oct = 0;
     TRay r;
     Hit best;
+    float best_det = 1.0f;  // any-hit queries: best.u, best.v hold V, W of the world hit until the ray is done
     AnyCtx ctx{0, 0, 0, 0};
     float tmin = 0.0f, tmax = 0.0f;
     uint2 ng = make_uint2(0, 0);
@@ -231,6 +248,7 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
                         load(q, o, d, tmin, tmax, ctx);
                         best.t = tmax;
                         best.u = best.v = 0.0f;
+                        best_det = 1.0f;
                         best.inst = best.prim = best.bgeo = 0xFFFFFFFFu;
                         iter = 0;
                         if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) {
@@ -279,17 +297,26 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
                 const TriRec* tr = s.cw_tris + tb + tbit;
                 const float4 pa = __ldg(&tr->a), pb = __ldg(&tr->b), pc = __ldg(&tr->c);
                 ts.tris++;
-                float t, u, v;
-                if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                // any-hit queries keep V, W and det of the hit and divide once the ray is done (if
+                // their caller reads u, v at all); closest-hit queries divide per accepted hit
+                float t, u, v, det = 1.0f;
+                if constexpr (kAny) {
+                    if (!isect_tri_t(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v, det)) continue;
+                } else {
+                    if (!isect_tri(r, f3(pa), f3(pb), f3(pc), tmin, best.t, t, u, v)) continue;
+                }
                 const uint32_t inst = __float_as_uint(pa.w);
                 const uint32_t prim = __float_as_uint(pb.w);
                 const uint32_t gw = __float_as_uint(pc.w);
                 if (!closer(t, inst, prim, best)) continue;
-                if (test_alpha && !(gw >> 31) && anyhit_ignore(s, s.inst[inst].custom, prim, inst, u, v, ctx))
+                if (test_alpha && !(gw >> 31) &&
+                    anyhit_ignore(s, s.inst[inst].custom, prim, inst, kAny ? __fdiv_rn(u, det) : u,
+                                  kAny ? __fdiv_rn(v, det) : v, ctx))
                     continue;
                 best.t = t;
                 best.u = u;
                 best.v = v;
+                best_det = det;
                 best.inst = inst;
                 best.prim = prim;
                 best.bgeo = gw & 0x7FFFFFFFu;
@@ -300,6 +327,10 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
             }
         }
         if (done) {
+            if constexpr (kAny) {
+                best.u = __fdiv_rn(best.u, best_det);
+                best.v = __fdiv_rn(best.v, best_det);
+            }
             if constexpr (kTlas) {
                 if (s.has_tlas && !(kAny && best.inst != 0xFFFFFFFFu))
                     trace_tlas<kAny, true>(s, r, r.o, r.d, tmin, best, test_alpha, ctx, ts);

@@ -46,9 +46,13 @@ GB_D void setup_ray(TRay& r, float3 o, float3 d) {
 }
 
 // Watertight ray-triangle test (FP32, IEEE round-to-nearest, no contraction
-// except the six projections, which are explicit FMAs on both sides).
-GB_D bool isect_tri(const TRay& r, float3 p0, float3 p1, float3 p2, float tmin, float tmax, float& t_out,
-                    float& u_out, float& v_out) {
+// except the six projections, which are explicit FMAs on both sides), up to
+// the distance: on a hit in [tmin, tmax] it returns t and the unnormalised
+// barycentrics V, W and their sum det with U; the barycentrics of the hit
+// are u = V / det, v = W / det (isect_tri), which a traversal loop divides
+// out only for the hit it keeps.
+GB_D bool isect_tri_t(const TRay& r, float3 p0, float3 p1, float3 p2, float tmin, float tmax, float& t_out,
+                      float& V_out, float& W_out, float& det_out) {
     float3 A = f3(sub_rn(p0.x, r.o.x), sub_rn(p0.y, r.o.y), sub_rn(p0.z, r.o.z));
     float3 B = f3(sub_rn(p1.x, r.o.x), sub_rn(p1.y, r.o.y), sub_rn(p1.z, r.o.z));
     float3 C = f3(sub_rn(p2.x, r.o.x), sub_rn(p2.y, r.o.y), sub_rn(p2.z, r.o.z));
@@ -75,6 +79,15 @@ GB_D bool isect_tri(const TRay& r, float3 p0, float3 p1, float3 p2, float tmin, 
     const float t = __fdiv_rn(T, det);
     if (!(t >= tmin && t <= tmax)) return false;
     t_out = t;
+    V_out = V;
+    W_out = W;
+    det_out = det;
+    return true;
+}
+GB_D bool isect_tri(const TRay& r, float3 p0, float3 p1, float3 p2, float tmin, float tmax, float& t_out,
+                    float& u_out, float& v_out) {
+    float V, W, det;
+    if (!isect_tri_t(r, p0, p1, p2, tmin, tmax, t_out, V, W, det)) return false;
     u_out = __fdiv_rn(V, det);
     v_out = __fdiv_rn(W, det);
     return true;
