@@ -42,12 +42,12 @@ TRS takes the channel's output and the world transforms are recomputed; a
 skin's joint matrices are world(joint) x inverse bind matrix, column-major,
 256 slots with zero matrices past the last joint.
 
-Normal-mapped primitives without tangents get generated ones
-(generate_tangents; the reference runs MikkTSpace there, geometry.rs:197-212);
+Primitives whose material has a normal texture and that carry no TANGENT
+attribute get MikkTSpace tangents (mikktspace.py, as the reference's
+generate_tangents call, geometry.rs:192-212, with its w convention);
 textures may be PNG or baseline JPEG (jpeg.py).  Morph targets are ignored,
 as in the reference (animation.rs:141-142), and so are glTF cameras (the
-reference's camera comes from its viewer).  Not reproduced: MikkTSpace's
-exact vertex splitting and degenerate rules.
+reference's camera comes from its viewer).
 """
 import base64
 import json
@@ -56,6 +56,7 @@ import struct
 
 import numpy as np
 
+from . import mikktspace
 from . import types as T
 from .scenes import GeoBuilder, SceneData, identity_instances
 
@@ -262,54 +263,6 @@ def _linear_images(doc):
     return lin
 
 
-def generate_tangents(pos, nrm, uv, tri):
-    """Per-vertex tangents (xyz, handedness w) for a normal-mapped primitive
-    that has none, where the reference runs MikkTSpace (geometry.rs:197-212).
-    Per triangle, tangent and bitangent follow from the UV gradients
-    (Lengyel's method); each corner adds them weighted by its angle; the sum
-    is made orthogonal to the vertex normal and normalised, and w is the sign
-    that makes cross(normal, tangent) * w point along the bitangent.  For
-    smooth, consistently mapped meshes this is MikkTSpace's result up to
-    rounding; its vertex splitting at UV seams and its degenerate-triangle
-    rules are not reproduced."""
-    pos = np.asarray(pos, np.float64)
-    nrm = np.asarray(nrm, np.float64)
-    uv = np.asarray(uv, np.float64)
-    tri = np.asarray(tri, np.int64).reshape(-1, 3)
-    n = len(pos)
-    t_acc, b_acc = np.zeros((n, 3)), np.zeros((n, 3))
-    p0, p1, p2 = pos[tri[:, 0]], pos[tri[:, 1]], pos[tri[:, 2]]
-    w0, w1, w2 = uv[tri[:, 0]], uv[tri[:, 1]], uv[tri[:, 2]]
-    e1, e2 = p1 - p0, p2 - p0
-    d1, d2 = w1 - w0, w2 - w0
-    r = d1[:, 0] * d2[:, 1] - d2[:, 0] * d1[:, 1]
-    ok = np.abs(r) > 1e-20
-    inv = np.where(ok, 1.0 / np.where(ok, r, 1.0), 0.0)[:, None]
-    tf = (e1 * d2[:, 1:2] - e2 * d1[:, 1:2]) * inv
-    bf = (e2 * d1[:, 0:1] - e1 * d2[:, 0:1]) * inv
-
-    def angle(a, b_, c):  # angle at a between edges a->b and a->c
-        u, v = b_ - a, c - a
-        nu, nv = np.linalg.norm(u, axis=1), np.linalg.norm(v, axis=1)
-        cosang = np.einsum("ij,ij->i", u, v) / np.maximum(nu * nv, 1e-30)
-        return np.arccos(np.clip(cosang, -1.0, 1.0))
-
-    for k, (a, b_, c) in enumerate(((p0, p1, p2), (p1, p2, p0), (p2, p0, p1))):
-        wgt = angle(a, b_, c)[:, None]
-        np.add.at(t_acc, tri[:, k], tf * wgt)
-        np.add.at(b_acc, tri[:, k], bf * wgt)
-    nn = nrm / np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
-    t = t_acc - nn * np.einsum("ij,ij->i", nn, t_acc)[:, None]
-    tl = np.linalg.norm(t, axis=1)
-    # no usable UV gradient: any unit vector perpendicular to the normal
-    alt = np.where(np.abs(nn[:, :1]) < 0.9, np.array([[1.0, 0.0, 0.0]]), np.array([[0.0, 1.0, 0.0]]))
-    alt = alt - nn * np.einsum("ij,ij->i", nn, alt)[:, None]
-    t = np.where(tl[:, None] > 1e-12, t, alt)
-    t /= np.maximum(np.linalg.norm(t, axis=1, keepdims=True), 1e-30)
-    w = np.where(np.einsum("ij,ij->i", np.cross(nn, t), b_acc) < 0.0, -1.0, 1.0)
-    return np.concatenate([t, w[:, None]], 1).astype(np.float32)
-
-
 def _textures(doc, bufs, base):
     from .jpeg import read_jpeg
     from .png import read_png
@@ -384,8 +337,10 @@ def load(path, light_seed=0):
                 color = np.concatenate([c, np.ones((n, 1), np.float32)], 1) if c.shape[1] == 3 else c
             tangent = get("TANGENT", 4)
             mat_raw = mats[p.get("material", 0)] if mats else {}
-            if tangent is None and "TEXCOORD_0" in attrs and "normalTexture" in mat_raw:
-                tangent = generate_tangents(pos, nrm, get("TEXCOORD_0", 2), idx.reshape(-1, 3))
+            if tangent is None and "normalTexture" in mat_raw:  # uv0 defaults to zeros, as in geometry.rs:182-185
+                uv0 = get("TEXCOORD_0", 2)
+                tangent = mikktspace.tangents(pos, nrm, uv0 if uv0 is not None else np.zeros((n, 2), np.float32),
+                                              idx.reshape(-1, 3))
             base_v = b.add_vertices(pos, nrm, uv=get("TEXCOORD_0", 2), color=color, tangent=tangent,
                                     joints=_accessor(doc, bufs, attrs["JOINTS_0"]).astype(np.uint32)
                                     if "JOINTS_0" in attrs else None,

@@ -210,26 +210,64 @@ def test_cubemap_faces(tmp_path):
     assert [int(data[k * 64]) for k in range(6)] == [0, 10, 20, 30, 40, 50]
 
 
-def test_generated_tangents():
-    """Tangents for normal-mapped primitives without a TANGENT attribute:
-    along +u of the texture mapping, orthogonal to the normal, unit length,
-    with the handedness of the v direction."""
-    from rustracer_gb300.gltf import generate_tangents
+def test_mikktspace_tangents():
+    """MikkTSpace tangents (mikktspace.py) for normal-mapped primitives
+    without a TANGENT attribute: along +u of the mapping, orthogonal to the
+    normal, unit length; w as the reference's set_tangent writes it (-1
+    where the mapping preserves orientation, geometry.rs:333-349)."""
+    from rustracer_gb300 import mikktspace
     pos = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32)
     nrm = np.tile([[0, 0, 1]], (4, 1)).astype(np.float32)
     tri = np.array([[0, 1, 2], [0, 2, 3]])
     uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
-    t = generate_tangents(pos, nrm, uv, tri)
-    assert np.allclose(t, [[1, 0, 0, 1]] * 4, atol=1e-6)
-    t = generate_tangents(pos, nrm, uv[:, ::-1], tri)  # u along +y, v along +x: mirrored mapping
-    assert np.allclose(t[:, :3], [[0, 1, 0]] * 4, atol=1e-6) and np.all(t[:, 3] == -1)
-    # a sphere with longitude / latitude mapping: unit tangents orthogonal to the normals
+    assert np.allclose(mikktspace.tangents(pos, nrm, uv, tri), [[1, 0, 0, -1]] * 4, atol=1e-6)
+    t = mikktspace.tangents(pos, nrm, uv[:, ::-1], tri)  # u along +y, v along +x: mirrored mapping
+    assert np.allclose(t, [[0, 1, 0, 1]] * 4, atol=1e-6)
+    # no texture coordinates (zeros): every triangle may join any group, none starts one
+    assert np.array_equal(mikktspace.tangents(pos, nrm, np.zeros((4, 2)), tri), [[1, 0, 0, 1]] * 4)
+    # a vertex no triangle names keeps the loader's default
+    t = mikktspace.tangents(np.r_[pos, [[5, 5, 5]]], np.r_[nrm, [[0, 0, 1]]], np.r_[uv, [[0, 0]]], tri)
+    assert np.array_equal(t[4], [1, 0, 0, 0])
+    # duplicated vertices with equal attributes are welded: same result as the shared quad
+    dpos, dnrm, duv = pos[[0, 1, 2, 0, 2, 3]], nrm[[0, 1, 2, 0, 2, 3]], uv[[0, 1, 2, 0, 2, 3]]
+    assert np.allclose(mikktspace.tangents(dpos, dnrm, duv, [[0, 1, 2], [3, 4, 5]]), [[1, 0, 0, -1]] * 6, atol=1e-6)
+    # the corner angle weights the sum: a vertex shared by a triangle mapped along +x and one
+    # mapped diagonally takes the angle-weighted mean of the two directions
+    # (corner angles 135 and 90 degrees; tangents (1, 0, 0) and (1, 1, 0) / sqrt 2)
+    p2 = np.array([[0, 0, 0], [1, -1, 0], [0, 1, 0], [-1, 0, 0]], np.float32)
+    u2 = np.array([[0, 0], [1, -1], [0, 1], [-1, 1]], np.float32)
+    n2 = np.tile([[0, 0, 1]], (4, 1)).astype(np.float32)
+    t = mikktspace.tangents(p2, n2, u2, [[0, 1, 2], [0, 2, 3]])
+    want = 0.75 * np.pi * np.array([1, 0, 0]) + 0.5 * np.pi * np.array([1, 1, 0]) / np.sqrt(2)
+    assert np.allclose(t[0], np.r_[want / np.linalg.norm(want), -1], atol=1e-6)
+    # mirrored halves sharing seam vertices: the two orientations form separate groups and the
+    # face that names a vertex last decides it
+    p3 = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [2, 0, 0], [2, 1, 0]], np.float32)
+    u3 = np.array([[0, 0], [1, 0], [1, 1], [0, 1], [0, 0], [0, 1]], np.float32)  # right half mirrored in u
+    n3 = np.tile([[0, 0, 1]], (6, 1)).astype(np.float32)
+    t = mikktspace.tangents(p3, n3, u3, [[0, 1, 2], [0, 2, 3], [1, 4, 5], [1, 5, 2]])
+    assert np.allclose(t[[0, 3]], [[1, 0, 0, -1]] * 2, atol=1e-6)
+    assert np.allclose(t[[1, 2, 4, 5]], [[-1, 0, 0, 1]] * 4, atol=1e-6)
+    t = mikktspace.tangents(p3, n3, u3, [[1, 4, 5], [1, 5, 2], [0, 1, 2], [0, 2, 3]])
+    assert np.allclose(t[[0, 1, 2, 3]], [[1, 0, 0, -1]] * 4, atol=1e-6)
+    # a degenerate triangle (two equal positions) copies the first healthy corner of its vertex;
+    # its other corners keep the default tangent space ((1, 0, 0), orientation not preserved)
+    p4 = np.r_[pos, [[3, 3, 3], [3, 3, 3]]]
+    t = mikktspace.tangents(p4, np.r_[nrm, nrm[:2]], np.r_[uv, [[0, 0], [0, 0]]], [[0, 1, 2], [0, 2, 3], [2, 4, 5]])
+    assert np.allclose(t[2], [1, 0, 0, -1], atol=1e-6) and np.array_equal(t[4:], [[1, 0, 0, 1]] * 2)
+    # a sphere with longitude / latitude mapping: unit tangents orthogonal to the normals, along
+    # the direction in which u grows
     from rustracer_gb300.scenes import _icosphere
     v, f = _icosphere(2)
+    v = v.astype(np.float32)
     uvs = np.stack([np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi) + 0.5, np.arccos(np.clip(v[:, 1], -1, 1)) / np.pi], 1)
-    t = generate_tangents(v, v, uvs, f)
+    t = mikktspace.tangents(v, v, uvs, f)
     assert np.allclose(np.linalg.norm(t[:, :3], axis=1), 1.0, atol=1e-5)
     assert np.abs(np.einsum("ij,ij->i", t[:, :3], v)).max() < 1e-4
+    du = np.stack([-v[:, 2], np.zeros(len(v)), v[:, 0]], 1)  # d(position)/d(longitude)
+    ok = np.linalg.norm(du, axis=1) > 0.3  # away from the poles
+    cosang = np.einsum("ij,ij->i", t[ok, :3], du[ok]) / np.linalg.norm(du[ok], axis=1)
+    assert np.median(cosang) > 0.99
 
 
 def test_loader_generates_tangents_for_normal_maps(tmp_path):
@@ -246,7 +284,7 @@ def test_loader_generates_tangents_for_normal_maps(tmp_path):
     doc["materials"][0]["normalTexture"] = {"index": 0}
     json.dump(doc, open(path, "w"))
     mapped = gltf.load(str(path))
-    assert np.allclose(mapped.vertices["tangent"][:4], [[1, 0, 0, 1]] * 4, atol=1e-6)
+    assert np.allclose(mapped.vertices["tangent"][:4], [[1, 0, 0, -1]] * 4, atol=1e-6)
 
 
 def _asset_fixture():
