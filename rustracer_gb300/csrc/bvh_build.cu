@@ -210,7 +210,8 @@ __device__ __forceinline__ float half_area(float3 l, float3 h) {
 __global__ void bottom_up_kernel(int n, const uint32_t* idx, const float4* lo, const float4* hi,
                                  const int32_t* left, const int32_t* right, const int32_t* parent_i,
                                  const int32_t* parent_l, const uint32_t* rlo, const uint32_t* rhi, float4* ilo,
-                                 float4* ihi, float* cost, uint32_t* collapse, uint32_t* arrive, uint32_t max_leaf) {
+                                 float4* ihi, float* cost, uint32_t* collapse, uint32_t* arrive, uint32_t max_leaf,
+                                 float cost_traverse) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int p = parent_l[i];
@@ -237,7 +238,7 @@ __global__ void bottom_up_kernel(int n, const uint32_t* idx, const float4* lo, c
         const float3 l = fmin3(bl[0], bl[1]), h = fmax3(bh[0], bh[1]);
         const float a = half_area(l, h);
         const uint32_t count = rhi[p] - rlo[p] + 1u;
-        const float split = kCostTraverse * a + c[0] + c[1];
+        const float split = cost_traverse * a + c[0] + c[1];
         const float as_leaf = kCostTri * a * (float)count;
         const bool col = count <= max_leaf && as_leaf <= split;
         ilo[p] = f4(l, 0.0f);
@@ -357,9 +358,11 @@ namespace {
 
 // Morton codes, sort, binary tree (PLOC clustering, or the Karras radix tree
 // when quality is kBvhFast) and the bottom-up pass (boxes, SAH costs, leaf
-// collapse with at most max_leaf items).  Item boxes in s.lo/hi and centroid
+// collapse with at most max_leaf items, an inner node costing cost_traverse
+// triangle tests per unit of area).  Item boxes in s.lo/hi and centroid
 // bounds in s.cbounds must be ready.
-cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t st, int quality) {
+cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t st, int quality,
+                       float cost_traverse = kCostTraverse) {
     morton_kernel<<<blocks(n), 256, 0, st>>>(s.lo, s.hi, n, s.cbounds, s.morton_in, s.idx_in);
     CK(cudaGetLastError());
     CK(cub::DeviceRadixSort::SortPairs(s.cub_tmp, s.cub_bytes, s.morton_in, s.morton, s.idx_in, s.idx, (int)n, 0,
@@ -375,7 +378,7 @@ cudaError_t radix_tree(Scratch& s, uint32_t n, uint32_t max_leaf, cudaStream_t s
         CK(cudaMemsetAsync(s.arrive, 0, (n - 1) * sizeof(uint32_t), st));
         bottom_up_kernel<<<blocks(n), 256, 0, st>>>((int)n, s.idx, s.lo, s.hi, s.left, s.right, s.parent_i,
                                                    s.parent_l, s.range_lo, s.range_hi, s.ilo, s.ihi, s.cost,
-                                                   s.collapse, s.arrive, max_leaf);
+                                                   s.collapse, s.arrive, max_leaf, cost_traverse);
         CK(cudaGetLastError());
     }
     return cudaSuccess;
