@@ -35,11 +35,11 @@ constexpr uint32_t kRefill = GBRT_REFILL;  // idle lanes that trigger a refill
 
 // Loader: bool load(uint32_t q, float3& o, float3& d, float& tmin, float& tmax, AnyCtx& ctx)
 // Finisher: void finish(uint32_t q, bool hit, const Hit& h)
-template <bool kAny, class Loader, class Finisher>
+template <bool kAny, bool kAlpha, class Loader, class Finisher>
 GB_D void persistent_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts,
                            Loader&& load, Finisher&& finish) {
     const uint32_t lane = threadIdx.x & 31u;
-    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+    const bool test_alpha = kAlpha && !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
     int stack_node[kStack];
     float stack_t[kStack];
     bool has = false, exhausted = false;
@@ -201,11 +201,11 @@ namespace gbrt {
 
 // Persistent-lane traversal of the 8-wide world BVH; same interface and
 // refill policy as persistent_trace.
-template <bool kAny, bool kTlas, class Loader, class Finisher>
+template <bool kAny, bool kTlas, bool kAlpha, class Loader, class Finisher>
 GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts,
                               Loader&& load, Finisher&& finish) {
     const uint32_t lane = threadIdx.x & 31u;
-    const bool test_alpha = !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
+    const bool test_alpha = kAlpha && !(flags & GBRT_RAY_OPAQUE) && !s.all_opaque;
 #if GBRT_CW_SMEM_STACK
     // the top kSmemStack entries of each lane's stack in shared memory ([entry][thread]: a warp's accesses
     // to one depth are consecutive 8-byte words), deeper ones in local memory; every traversal kernel
@@ -346,13 +346,18 @@ GB_D void persistent_trace_cw(const DevScene& s, uint32_t n, uint32_t* work, uin
 //   kTraceWide    8-wide world BVH, no transformed instances
 //   kTraceWideTlas 8-wide world BVH, then the TLAS with 8-wide BLASes
 // Keeping the TLAS code out of the common form keeps its registers free.
-constexpr int kTraceBinary = 0, kTraceWide = 1, kTraceWideTlas = 2;
+// A form | kTraceOpaque is compiled without the any-hit alpha test, for
+// launches where no geometry can need it (all-opaque scenes or frames); the
+// code it leaves out cost the 8-wide traversal kernels spills.
+constexpr int kTraceBinary = 0, kTraceWide = 1, kTraceWideTlas = 2, kTraceOpaque = 4;
 
 template <bool kAny, int kMode, class Loader, class Finisher>
 GB_D void world_trace(const DevScene& s, uint32_t n, uint32_t* work, uint32_t flags, TraceStats& ts, Loader&& load,
                       Finisher&& finish) {
-    if constexpr (kMode == kTraceBinary) persistent_trace<kAny>(s, n, work, flags, ts, load, finish);
-    else persistent_trace_cw<kAny, kMode == kTraceWideTlas>(s, n, work, flags, ts, load, finish);
+    constexpr int kForm = kMode & 3;
+    constexpr bool kAlpha = !(kMode & kTraceOpaque);
+    if constexpr (kForm == kTraceBinary) persistent_trace<kAny, kAlpha>(s, n, work, flags, ts, load, finish);
+    else persistent_trace_cw<kAny, kForm == kTraceWideTlas, kAlpha>(s, n, work, flags, ts, load, finish);
 }
 
 // The form a scene needs: binary when it has a world BVH without its

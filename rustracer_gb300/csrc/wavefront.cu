@@ -101,6 +101,20 @@ cudaError_t init_wavefront_constants(const float* srgb_lut) {
     return cudaMemcpyToSymbol(c_srgb_lut, srgb_lut, 256 * sizeof(float));
 }
 
+// Launches traversal kernel K in the form `mode` (trace_mode, with
+// kTraceOpaque when nothing in the launch can need the alpha test).
+#define GBRT_TRACE_LAUNCH(K, grid, strm, ...)                                                       \
+    switch (mode) {                                                                                 \
+        case kTraceWide: K<kTraceWide><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;                 \
+        case kTraceWideTlas: K<kTraceWideTlas><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;         \
+        case kTraceBinary: K<kTraceBinary><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;             \
+        case kTraceWide | kTraceOpaque: K<kTraceWide | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break; \
+        case kTraceWideTlas | kTraceOpaque:                                                         \
+            K<kTraceWideTlas | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__);                  \
+            break;                                                                                  \
+        default: K<kTraceBinary | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;        \
+    }
+
 namespace {
 struct Grid {
     int dev = -1;
@@ -215,7 +229,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
     J.flags = ubo.fully_opaque ? GBRT_RAY_OPAQUE : 0u;
     J.tfar = ubo.orthographic_fov_dis > 0.0f ? 100000.0f : 10000.0f;
     J.path0 = 0;
-    const int mode = trace_mode(s);
+    const int mode = trace_mode(s) | (s.all_opaque || ubo.fully_opaque ? kTraceOpaque : 0);
     // the shade form: the scene's material features and this frame's debug settings
     const uint32_t feat = s.shade_feat | (ubo.mapping != 0u || ubo.debug == 1u ? kFeatDebug : 0u);
     // waves: k samples of a pixel range, k * npw <= cap
@@ -238,9 +252,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
             te();
             for (uint32_t b = 0; b < nb; ++b) {
                 tb(0);
-                if (mode == kTraceWide) wf_extend<kTraceWide><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
-                else if (mode == kTraceWideTlas) wf_extend<kTraceWideTlas><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
-                else wf_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(w, st, b);
+                GBRT_TRACE_LAUNCH(wf_extend, g_grid.extend, stream, w, st, b);
                 te();
                 if (side && b > 0 && (e = cudaStreamWaitEvent(stream, side->shadowed, 0)) != cudaSuccess) return e;
                 tb(1);
@@ -263,9 +275,7 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
                     if ((e = cudaStreamWaitEvent(side->stream, side->shaded, 0)) != cudaSuccess) return e;
                     ss = side->stream;
                 }
-                if (mode == kTraceWide) wf_shadow<kTraceWide><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
-                else if (mode == kTraceWideTlas) wf_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
-                else wf_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, ss>>>(w, st, b);
+                GBRT_TRACE_LAUNCH(wf_shadow, g_grid.shadow, ss, w, st, b);
                 if (side && (e = cudaEventRecord(side->shadowed, ss)) != cudaSuccess) return e;
                 te();
             }
