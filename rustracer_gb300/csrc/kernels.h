@@ -83,9 +83,10 @@ struct WaveRing {
     WaveDesc* host = nullptr;
     cudaEvent_t ev[kSlots] = {};
     int next = 0;
-    // captured launch sequences of batched waves, per traversal form and
-    // bounce count, valid for the wavefront buffers in graph_state
-    cudaGraphExec_t graph[3][32] = {};
+    // captured launch sequences of batched waves, per traversal form (with
+    // or without kTraceOpaque) and bounce count, valid for the wavefront
+    // buffers in graph_state
+    cudaGraphExec_t graph[8][32] = {};
     WfState graph_state{};
 };
 // Drops the captured graphs (the ring's buffers stay).

@@ -180,7 +180,11 @@ int wave_mode(const WaveDesc& w) {
         if (m == kTraceBinary) mode = kTraceBinary;
         else if (m == kTraceWideTlas && mode == kTraceWide) mode = kTraceWideTlas;
     }
-    return mode;
+    // the alpha test is compiled out when no job of the wave can need it
+    bool opaque = true;
+    for (uint32_t j = 0; j < w.njobs; ++j)
+        opaque = opaque && (w.jobs[j].s.all_opaque || (w.jobs[j].flags & GBRT_RAY_OPAQUE));
+    return mode | (opaque ? kTraceOpaque : 0);
 }
 
 // The launches of one batched wave with `nb` bounces in traversal form
@@ -203,17 +207,13 @@ cudaError_t enqueue_wave(const WfState& st, int mode, uint32_t nb, cudaStream_t 
     te();
     for (uint32_t b = 0; b < nb; ++b) {
         tb(0);
-        if (mode == kTraceWide) wfm_extend<kTraceWide><<<g_grid.extend, 128, 0, stream>>>(st, b);
-        else if (mode == kTraceWideTlas) wfm_extend<kTraceWideTlas><<<g_grid.extend, 128, 0, stream>>>(st, b);
-        else wfm_extend<kTraceBinary><<<g_grid.extend, 128, 0, stream>>>(st, b);
+        GBRT_TRACE_LAUNCH(wfm_extend, g_grid.extend, stream, st, b);
         te();
         tb(1);
         wfm_shade<<<g_grid.shade, kShadeThreads, 0, stream>>>(st, b);
         te();
         tb(2);
-        if (mode == kTraceWide) wfm_shadow<kTraceWide><<<g_grid.shadow, 128, 0, stream>>>(st, b);
-        else if (mode == kTraceWideTlas) wfm_shadow<kTraceWideTlas><<<g_grid.shadow, 128, 0, stream>>>(st, b);
-        else wfm_shadow<kTraceBinary><<<g_grid.shadow, 128, 0, stream>>>(st, b);
+        GBRT_TRACE_LAUNCH(wfm_shadow, g_grid.shadow, stream, st, b);
         te();
     }
     tb(3);

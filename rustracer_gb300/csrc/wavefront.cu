@@ -101,20 +101,6 @@ cudaError_t init_wavefront_constants(const float* srgb_lut) {
     return cudaMemcpyToSymbol(c_srgb_lut, srgb_lut, 256 * sizeof(float));
 }
 
-// Launches traversal kernel K in the form `mode` (trace_mode, with
-// kTraceOpaque when nothing in the launch can need the alpha test).
-#define GBRT_TRACE_LAUNCH(K, grid, strm, ...)                                                       \
-    switch (mode) {                                                                                 \
-        case kTraceWide: K<kTraceWide><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;                 \
-        case kTraceWideTlas: K<kTraceWideTlas><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;         \
-        case kTraceBinary: K<kTraceBinary><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;             \
-        case kTraceWide | kTraceOpaque: K<kTraceWide | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break; \
-        case kTraceWideTlas | kTraceOpaque:                                                         \
-            K<kTraceWideTlas | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__);                  \
-            break;                                                                                  \
-        default: K<kTraceBinary | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;        \
-    }
-
 namespace {
 struct Grid {
     int dev = -1;

@@ -32,6 +32,20 @@
 // Same bound for every traversal form.
 constexpr int trace_minb(int) { return GBRT_TRACE_MINB; }
 
+// Launches traversal kernel K in the form `mode` (trace_mode, with
+// kTraceOpaque when nothing in the launch can need the alpha test).
+#define GBRT_TRACE_LAUNCH(K, grid, strm, ...)                                                       \
+    switch (mode) {                                                                                 \
+        case kTraceWide: K<kTraceWide><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;                 \
+        case kTraceWideTlas: K<kTraceWideTlas><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;         \
+        case kTraceBinary: K<kTraceBinary><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;             \
+        case kTraceWide | kTraceOpaque: K<kTraceWide | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break; \
+        case kTraceWideTlas | kTraceOpaque:                                                         \
+            K<kTraceWideTlas | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__);                  \
+            break;                                                                                  \
+        default: K<kTraceBinary | kTraceOpaque><<<grid, 128, 0, strm>>>(__VA_ARGS__); break;        \
+    }
+
 // With the ray-sort key, shadow rays are grouped by octant too; shade blocks
 // of 256 threads make the groups twice as long (icosphere frame: 3719 Mrays/s
 // with neither, 3748 with both).
