@@ -143,6 +143,7 @@ uint32_t material_features(const gbrt_material_raw* mats, uint32_t nmat) {
             if (t->index >= 0) f |= gbrt::kFeatTextures;
         if (m.workflow == 1u) f |= gbrt::kFeatSpecGloss;
         if (m.unlit) f |= gbrt::kFeatDebug;
+        if (m.volume_exists) f |= gbrt::kFeatVolume;
     }
     return f;
 }

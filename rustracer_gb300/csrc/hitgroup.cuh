@@ -90,6 +90,7 @@ template <uint32_t kFeat = kFeatAll, class ShadowFn>
 GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const Hit& h, float3 wdir, PathStats& ps,
                       ShadowFn&& shadow) {
     constexpr bool kTex = (kFeat & kFeatTextures) != 0;
+    constexpr bool kVol = (kFeat & kFeatVolume) != 0;
     ps.shaded++;
     const DevInstance& in = s.inst[h.inst];
     const uint32_t custom = in.custom;
@@ -222,7 +223,7 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
     }
     m.attenuation_color = f3(mat.attenuation_color[0], mat.attenuation_color[1], mat.attenuation_color[2]);
     m.attenuation_distance = mat.attenuation_distance;
-    m.volume = mat.volume_exists != 0;
+    m.volume = kVol && mat.volume_exists != 0;
     const float displacement = len3(origin - last_hit);
 
     gbrt_light_raw light;
@@ -251,7 +252,7 @@ GB_D void closest_hit(const DevScene& s, const gbrt_ubo& ubo, Payload& R, const 
             if (R.volume_dis >= 0.0f) R.volume_dis += displacement;
         } else {
             type = TRANSMISSION_TYPE;
-            if (mat.volume_exists) {
+            if (kVol && mat.volume_exists) {
                 if (R.volume_dis >= 0.0f) R.volume_dis += displacement;
                 else if (frontFace) R.volume_dis = 0.0f;
             }

@@ -88,6 +88,9 @@ struct WaveRing {
     // buffers in graph_state
     cudaGraphExec_t graph[8][32] = {};
     WfState graph_state{};
+    // private stream the graphs are captured on: the launch stream is shared
+    // with the API calls of other threads, which must not land in a capture
+    cudaStream_t cap = nullptr;
 };
 // Drops the captured graphs (the ring's buffers stay).
 void wave_graphs_reset(WaveRing& r);

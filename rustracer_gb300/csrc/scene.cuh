@@ -117,6 +117,7 @@ struct DevScene {
 constexpr uint32_t kFeatTextures = 1u;   // some material samples a texture
 constexpr uint32_t kFeatSpecGloss = 2u;  // some material uses the specular-glossiness workflow
 constexpr uint32_t kFeatDebug = 4u;      // unlit materials, a debug mapping or the legacy debug branch
-constexpr uint32_t kFeatAll = 7u;
+constexpr uint32_t kFeatVolume = 8u;     // some material has KHR_materials_volume (refraction, attenuation)
+constexpr uint32_t kFeatAll = 15u;
 
 }  // namespace gbrt

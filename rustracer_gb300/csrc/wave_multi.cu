@@ -120,6 +120,11 @@ cudaError_t wave_ring_init(WaveRing& r) {
             return e;
         }
     }
+    if ((e = cudaStreamCreateWithFlags(&r.cap, cudaStreamNonBlocking)) != cudaSuccess) {
+        r.cap = nullptr;
+        wave_ring_free(r);
+        return e;
+    }
     r.next = 0;
     return cudaSuccess;
 }
@@ -135,6 +140,8 @@ void wave_ring_free(WaveRing& r) {
     }
     if (r.host) cudaFreeHost(r.host);
     r.host = nullptr;
+    if (r.cap) cudaStreamDestroy(r.cap);
+    r.cap = nullptr;
 }
 
 cudaError_t wave_acquire(WaveRing& r, WaveDesc** slot) {
@@ -260,9 +267,9 @@ cudaError_t launch_wave(WaveRing& ring, const WfState& st, cudaStream_t stream, 
     cudaGraphExec_t& exec = ring.graph[mode][w.nb];
     if (!exec) {
         cudaGraph_t graph = nullptr;
-        if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        const cudaError_t ee = enqueue_wave(st, mode, w.nb, stream, nullptr);
-        e = cudaStreamEndCapture(stream, &graph);
+        if ((e = cudaStreamBeginCapture(ring.cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+        const cudaError_t ee = enqueue_wave(st, mode, w.nb, ring.cap, nullptr);
+        e = cudaStreamEndCapture(ring.cap, &graph);
         if (ee != cudaSuccess) e = ee;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
         if (graph) cudaGraphDestroy(graph);
