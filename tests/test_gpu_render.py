@@ -126,6 +126,27 @@ def test_headline_frame_band(gpu_ctx, band):
     assert c["n"] == (r1 - r0) * W * 2
 
 
+def test_unused_material_features_keep_the_bits(gpu_ctx):
+    """A material that no geometry uses but that has a texture, the
+    specular-glossiness workflow and a volume moves the frame from the
+    specialised shade kernel to the one with every feature compiled in; the
+    samples, hits and image stay bit-identical."""
+    import copy
+    from rustracer_gb300 import gbrt
+    sd = scenes.icosphere_scene(subdiv=3)
+    ubo = sd.ubo(64, 48, samples=4, bounces=8, exposure=1.0)
+    plain = render_gpu(gpu_ctx, sd, ubo, 64, 48, mode=gbrt.MODE_WAVEFRONT)
+    full = copy.deepcopy(sd)
+    extra = full.materials[:1].copy()
+    extra["workflow"] = 1
+    extra["volume_exists"] = 1
+    extra["base_color_texture"]["index"] = 0
+    full.materials = np.concatenate([full.materials, extra])
+    r = render_gpu(gpu_ctx, full, ubo, 64, 48, mode=gbrt.MODE_WAVEFRONT)
+    assert np.array_equal(r["samples"].view(np.uint32), plain["samples"].view(np.uint32))
+    assert np.array_equal(r["hits"], plain["hits"]) and np.array_equal(r["image"], plain["image"])
+
+
 def test_accumulation_across_frames(gpu_ctx):
     """Two frames of 2 spp accumulate like one frame of 4 spp (rgen:132-135)."""
     from rustracer_gb300 import gbrt
