@@ -197,12 +197,27 @@ GB_D void camera_body(const Wv& w, const WfState& st, uint32_t pid) {
     float3 o, d;
     float tfar;
     camera_ray(J.ubo, x, y, W, J.out.height, rng, seed, o, d, tfar);
-    st.ray_o[0][pid] = f4(o, 0.0f);
+    // .w of the origin: RandomSeed after the aperture draws.  The rest of the
+    // path state starts from values that shade of bounce 0 sets itself
+    // (initial_state), so it is not written here unless no bounce runs.
+    st.ray_o[0][pid] = f4(o, __uint_as_float(seed));
     st.ray_d[0][pid] = f4(d, __uint_as_float(pid | si << kPidBits));
-    st.tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);                   // throughput, Ray.t = 0
-    st.rad[pid] = f4(0.0f, 0.0f, 0.0f, -1.0f);                 // radiance, volume_dis = -1
-    st.hp[pid] = f4(0.0f, 0.0f, 0.0f, __uint_as_float(seed));  // hitPoint, RandomSeed
-    st.rng[pid] = make_uint4(rng.w, 0u, tea16(sample, 0x9E3779B9u), 0u);
+    if (J.ubo.number_of_bounces == 0u) {  // wf_finish reads radiance and Ray.t
+        st.tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);
+        st.rad[pid] = f4(0.0f, 0.0f, 0.0f, -1.0f);
+    }
+}
+
+// The path state a camera ray starts with: throughput 1 (Ray.t = 0),
+// radiance 0 (volume_dis = -1), hitPoint 0 with the RandomSeed the camera
+// left in the origin's .w, the pixel stream's counter after the camera's
+// anti-aliasing draws and the ray stream's seed (RayTracing.rgen:32-48, D1).
+GB_D void initial_state(const gbrt_ubo& ubo, float seed_bits, uint32_t sample, float4& tp, float4& rad, float4& hp,
+                        uint4& rg) {
+    tp = f4(1.0f, 1.0f, 1.0f, 0.0f);
+    rad = f4(0.0f, 0.0f, 0.0f, -1.0f);
+    hp = f4(0.0f, 0.0f, 0.0f, seed_bits);
+    rg = make_uint4(ubo.antialiasing ? 2u : 0u, 0u, tea16(sample, 0x9E3779B9u), 0u);
 }
 
 // traceRayEXT for the extension queue of bounce b (closest hit).
@@ -307,8 +322,16 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             const PathXY P = decode_path(w, word, J.out.width);
             const uint32_t pid = P.pid;
             const float4 h4 = st.hit[R + q];
-            const float4 tp4 = st.tp[pid], rad4 = st.rad[pid], hp4 = st.hp[pid];
-            uint4 rg = st.rng[pid];
+            float4 tp4, rad4, hp4;
+            uint4 rg;
+            if (b == 0u) {
+                initial_state(ubo, st.ray_o[0][R + q].w, P.sg->sample0 + P.j, tp4, rad4, hp4, rg);
+            } else {
+                tp4 = st.tp[pid];
+                rad4 = st.rad[pid];
+                hp4 = st.hp[pid];
+                rg = st.rng[pid];
+            }
             Payload Rp;
             Rp.hitValue = Rp.scatterDir = Rp.emittance = f3(0.0f);
             Rp.needScatter = 0;
