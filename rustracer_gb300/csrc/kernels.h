@@ -34,13 +34,12 @@ constexpr int kMaxWaveJobs = 32;                     // jobs sharing one wave
 constexpr int kMaxWaveSegs = kPidBits <= 24 ? 256 : (1 << (32 - kPidBits));  // (pixels x samples) pieces per wave
 struct WfState {
     uint32_t cap;
-    float4* ray_o[2];   // extension queues (ping-pong): origin
+    float4* ray_o[2];   // extension queues (ping-pong): origin (the path's hit point), RandomSeed in .w
     float4* ray_d[2];   //   direction, path id | segment << kPidBits in .w
     float4* hit;        // t, u, v, instance id
     uint32_t* hit_prim;
     float4* tp;         // per path: throughput, Ray.t
     float4* rad;        //   radiance, volume_dis
-    float4* hp;         //   hit point, RandomSeed
     uint4* rng;         //   pixel-stream counter, ray-stream counter, ray-stream z
     float4* sh_o;       // shadow queue: origin, tmax
     float4* sh_d;       //   direction, path id

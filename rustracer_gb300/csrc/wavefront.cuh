@@ -314,7 +314,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         float3 nxt_o = f3(0.0f), nxt_d = f3(0.0f), so = f3(0.0f), sd = f3(0.0f), sc = f3(0.0f), se = f3(0.0f);
         float3 tp_before = f3(0.0f);
         float stmax = 0.0f;
-        uint32_t word = 0;
+        uint32_t word = 0, nseed = 0;
         if (active) {
             const float4 d4 = rd[q];
             const float3 d = f3(d4);
@@ -326,10 +326,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             uint4 rg;
             if (b == 0u) {
                 initial_state(ubo, st.ray_o[0][R + q].w, P.sg->sample0 + P.j, tp4, rad4, hp4, rg);
-            } else {
+            } else {  // the hit point is this ray's origin, which carries RandomSeed
                 tp4 = st.tp[pid];
                 rad4 = st.rad[pid];
-                hp4 = st.hp[pid];
+                hp4 = st.ray_o[b & 1][R + q];
                 rg = st.rng[pid];
             }
             Payload Rp;
@@ -421,10 +421,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             if (stop_after) cont = false;
             st.tp[pid] = f4(tp, Rp.t);
             st.rad[pid] = f4(rad, Rp.volume_dis);
-            st.hp[pid] = f4(Rp.hitPoint, __uint_as_float(Rp.RandomSeed));
             st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
+            nseed = Rp.RandomSeed;
             }
         }
         uint32_t slot, sslot;
@@ -437,7 +437,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             sslot = warp_append(&cnt[kShadow + b], shadow);
         }
         if (cont) {
-            no[slot] = f4(nxt_o, 0.0f);
+            no[slot] = f4(nxt_o, __uint_as_float(nseed));
             nd[slot] = f4(nxt_d, __uint_as_float(word));
         }
         if (shadow) {
