@@ -43,12 +43,18 @@ struct WfState {
     uint4* rng;         //   pixel-stream counter, ray-stream counter, ray-stream z
     float4* sh_o;       // shadow queue: origin, tmax
     float4* sh_d;       //   direction, path id
-    float4* sh_e;       //   emission E, throughput.x
-    float4* sh_c;       //   NEE term C, throughput.y
-    float* sh_tp;       //   throughput.z
+    // the path's radiance (and volume_dis) after this vertex if the shadow ray
+    // is blocked / unblocked; in frames with a radiance cache (kShadowDelta)
+    // instead emission E + throughput.x / NEE term C + throughput.y, added to
+    // the radiance by the shadow kernel with throughput.z from sh_tp
+    float4* sh_e;
+    float4* sh_c;
+    float* sh_tp;
     uint32_t* counts;   // kMaxWaveJobs * kWfCounters queue lengths and fetch cursors
     float4* frame_sum;  // per pixel: sum of the frame's samples, last Ray.t (single-frame renders)
 };
+// WaveJob::flags bit: the job's shadow records hold deltas (sh_e / sh_c).
+constexpr uint32_t kShadowDelta = 0x80000000u;
 
 // One job of a wave: a scene, its UBO and its outputs.  The job's paths are
 // the contiguous range [path0, path0 + npaths) of the wave; its queues live
@@ -59,7 +65,7 @@ struct WaveJob {
     RenderOut out;
     float4* frame_sum;  // per pixel of the job's image
     uint32_t ns;        // samples of the frame (stride of the per-sample outputs)
-    uint32_t flags;     // GBRT_RAY_OPAQUE when the UBO says fully_opaque
+    uint32_t flags;     // GBRT_RAY_OPAQUE when the UBO says fully_opaque; kShadowDelta
     float tfar;
     uint32_t path0, npaths;
 };

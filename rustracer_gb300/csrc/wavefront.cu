@@ -212,7 +212,9 @@ cudaError_t launch_wavefront(const DevScene& s, const gbrt_ubo& ubo, const Rende
     J.out = out;
     J.frame_sum = st.frame_sum;
     J.ns = ns;
-    J.flags = ubo.fully_opaque ? GBRT_RAY_OPAQUE : 0u;
+    // a radiance cache adds to the radiance between shade and shadow (wf_nrc_apply), so the shadow
+    // records then hold deltas that the shadow kernel adds
+    J.flags = (ubo.fully_opaque ? GBRT_RAY_OPAQUE : 0u) | (nrc ? kShadowDelta : 0u);
     J.tfar = ubo.orthographic_fov_dis > 0.0f ? 100000.0f : 10000.0f;
     J.path0 = 0;
     const int mode = trace_mode(s) | (s.all_opaque || ubo.fully_opaque ? kTraceOpaque : 0);

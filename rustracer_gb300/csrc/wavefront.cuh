@@ -315,6 +315,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         float3 tp_before = f3(0.0f);
         float stmax = 0.0f;
         uint32_t word = 0, nseed = 0;
+        float4 sh_blocked = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh_lit = sh_blocked;  // radiance after this vertex, shadow ray blocked / not
         if (active) {
             const float4 d4 = rd[q];
             const float3 d = f3(d4);
@@ -420,7 +421,12 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             }
             if (stop_after) cont = false;
             st.tp[pid] = f4(tp, Rp.t);
-            st.rad[pid] = f4(rad, Rp.volume_dis);
+            if (kNrc || !shadow) {
+                st.rad[pid] = f4(rad, Rp.volume_dis);
+            } else {  // the shadow kernel writes the radiance: E + C when the light is visible (rchit:338-350)
+                sh_blocked = f4(rad + tp_before * se, Rp.volume_dis);
+                sh_lit = f4(rad + tp_before * (se + sc), Rp.volume_dis);
+            }
             st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
@@ -443,9 +449,14 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         if (shadow) {
             st.sh_o[R + sslot] = f4(so, stmax);
             st.sh_d[R + sslot] = f4(sd, __uint_as_float(word));
-            st.sh_e[R + sslot] = f4(se, tp_before.x);
-            st.sh_c[R + sslot] = f4(sc, tp_before.y);
-            st.sh_tp[R + sslot] = tp_before.z;
+            if constexpr (kNrc) {
+                st.sh_e[R + sslot] = f4(se, tp_before.x);
+                st.sh_c[R + sslot] = f4(sc, tp_before.y);
+                st.sh_tp[R + sslot] = tp_before.z;
+            } else {
+                st.sh_e[R + sslot] = sh_blocked;
+                st.sh_c[R + sslot] = sh_lit;
+            }
         }
     }
     const unsigned long long hs = warp_sum<unsigned long long>(ps.shaded);
@@ -478,9 +489,13 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
             }
         },
         [&](uint32_t q, bool occluded, const Hit&) {
-            const float4 d4 = sd[q], e4 = st.sh_e[R + q], c4 = st.sh_c[R + q];
+            const uint32_t pid = __float_as_uint(sd[q].w) & kPidMask;
+            if (!(J.flags & kShadowDelta)) {  // the record holds both outcomes
+                st.rad[pid] = occluded ? st.sh_e[R + q] : st.sh_c[R + q];
+                return;
+            }
+            const float4 e4 = st.sh_e[R + q], c4 = st.sh_c[R + q];
             const float tpz = st.sh_tp[R + q];
-            const uint32_t pid = __float_as_uint(d4.w) & kPidMask;
             float3 e = f3(e4);
             if (!occluded) e += f3(c4);
             const float4 r = st.rad[pid];
