@@ -427,7 +427,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 sh_blocked = f4(rad + tp_before * se, Rp.volume_dis);
                 sh_lit = f4(rad + tp_before * (se + sc), Rp.volume_dis);
             }
-            st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
+            if (cont) st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);  // read again only by a next bounce
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
             nseed = Rp.RandomSeed;
