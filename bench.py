@@ -595,7 +595,7 @@ def run_nrc(args):
     else:
         tuning = {"chosen_width": int(args.tune[1]), "sort_rays": int(args.tune.endswith("s"))}
         sc.set_tuning(tuning["chosen_width"], bool(tuning["sort_rays"]))
-    if args.judge == "cpu64":
+    if args.reference_image == "cpu64":
         # the oracle with FP64 intersection and accumulation on every host core, over
         # samples disjoint from the GPU runs' (global indices from 2^24 up)
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -607,7 +607,7 @@ def run_nrc(args):
                                                  bounces=depth, exposure=1.0, has_sky=True), Wn, Hn,
                                           accum=acc64, fp64=True, out=False)["stats"]
         ref = acc64.reshape(Hn, Wn, 4)[..., :3] / float(args.ref_spp)
-        judge = {"kind": "FP64-intersection CPU oracle", "spp": args.ref_spp, "seconds": round(time.time() - t0, 1),
+        ref_image = {"kind": "FP64-intersection CPU oracle", "spp": args.ref_spp, "seconds": round(time.time() - t0, 1),
                  "threads": int(ref_st["threads"]), "samples": f"global indices {off}..{off + args.ref_spp - 1}"}
     else:
         ref_acc = gbrt.Accum(ctx, Wn, Hn)
@@ -616,7 +616,7 @@ def run_nrc(args):
             sc.render(sd.ubo(Wn, Hn, samples=chunk, total=k + chunk, bounces=depth, exposure=1.0, has_sky=True),
                       ref_acc, image=False, mode=MODES["wavefront"])
         ref = ref_acc.download()[..., :3] / float(args.ref_spp)
-        judge = {"kind": "FP32 GPU path tracing (wavefront)", "spp": args.ref_spp}
+        ref_image = {"kind": "FP32 GPU path tracing (wavefront)", "spp": args.ref_spp}
     den = ref * ref + 1e-2
 
     def relmse(acc, spp):
@@ -675,7 +675,7 @@ def run_nrc(args):
             "data": "synthetic (seeded city block of instanced boxes and spheres)",
             "config": {"workload": f"city_nrc_{Wn}x{Hn}_depth{depth}", "instances": int(len(sd.instances)),
                        "instanced_triangles": int(sd.instanced_triangles), "point_lights": 16, "sky": True,
-                       "reference": judge,
+                       "reference": ref_image,
                        "cache": {"levels": 16, "table": 1 << 19, "features": 2, "mlp": "32-64x5-3 ReLU",
                                  "spp_per_frame": args.nrc_spp, "train_samples_per_frame": args.nrc_samples,
                                  "adam_steps_per_frame": args.nrc_steps, "lr": 1e-3,
@@ -752,7 +752,7 @@ def main():
                          "at 1-4 spp) of the same scenes")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--ref-spp", type=int, default=1024, help="nrc: samples of the reference image")
-    ap.add_argument("--judge", default="gpu32", choices=["gpu32", "cpu64"],
+    ap.add_argument("--reference-image", default="gpu32", choices=["gpu32", "cpu64"],
                     help="nrc: reference image from FP32 GPU path tracing, or from the FP64-intersection CPU "
                          "oracle (use with a small --res, e.g. 240x136)")
     ap.add_argument("--max-frames", type=int, default=200, help="nrc: frame limit of the plain run (x4 for the cache)")

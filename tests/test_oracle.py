@@ -320,7 +320,7 @@ def test_float_skybox_bilinear_texels():
 
 
 def test_city_fp32_and_fp64_intersection_agree():
-    """The radiance-cache workload's judge: on the city block (4,001
+    """The radiance-cache workload's reference image: on the city block (4,001
     flattened instances, sky, 16 lights) the oracle's FP32 render and its
     FP64-intersection, FP64-accumulation render of the same samples differ by
     a relMSE far below the 1e-2 convergence target, so a reference of N
