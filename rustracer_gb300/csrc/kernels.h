@@ -38,9 +38,11 @@ struct WfState {
     float4* ray_d[2];   //   direction, path id | segment << kPidBits in .w
     float4* hit;        // t, u, v, instance id
     uint32_t* hit_prim;
-    float4* tp;         // per path: throughput, Ray.t
-    float4* rad;        //   radiance, volume_dis
-    uint4* rng;         //   pixel-stream counter, ray-stream counter, ray-stream z
+    float4* q_tp[2];    // beside the extension queues: the path's throughput, Ray.t
+    uint4* q_rng[2];    //   pixel-stream counter, ray-stream counter, ray-stream z
+    float4* rad;        // per path: radiance, volume_dis (Ray.t once the path has ended)
+    float4* tp;         //   throughput, Ray.t, and
+    uint4* rng;         //   RNG counters, in frames with a radiance cache (which reads them by path id)
     float4* sh_o;       // shadow queue: origin, tmax
     float4* sh_d;       //   direction, path id
     // the path's radiance (and volume_dis) after this vertex if the shadow ray

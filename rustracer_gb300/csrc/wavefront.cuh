@@ -204,7 +204,7 @@ GB_D void camera_body(const Wv& w, const WfState& st, uint32_t pid) {
     st.ray_d[0][pid] = f4(d, __uint_as_float(pid | si << kPidBits));
     if (J.ubo.number_of_bounces == 0u) {  // wf_finish reads radiance and Ray.t
         st.tp[pid] = f4(1.0f, 1.0f, 1.0f, 0.0f);
-        st.rad[pid] = f4(0.0f, 0.0f, 0.0f, -1.0f);
+        st.rad[pid] = f4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
@@ -316,6 +316,8 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         float stmax = 0.0f;
         uint32_t word = 0, nseed = 0;
         float4 sh_blocked = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh_lit = sh_blocked;  // radiance after this vertex, shadow ray blocked / not
+        float4 q_tp_next = sh_blocked;  // throughput and Ray.t for the next bounce's queue
+        uint4 q_rng_next = make_uint4(0u, 0u, 0u, 0u);
         if (active) {
             const float4 d4 = rd[q];
             const float3 d = f3(d4);
@@ -328,10 +330,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             if (b == 0u) {
                 initial_state(ubo, st.ray_o[0][R + q].w, P.sg->sample0 + P.j, tp4, rad4, hp4, rg);
             } else {  // the hit point is this ray's origin, which carries RandomSeed
-                tp4 = st.tp[pid];
+                tp4 = kNrc ? st.tp[pid] : st.q_tp[b & 1][R + q];
                 rad4 = st.rad[pid];
                 hp4 = st.ray_o[b & 1][R + q];
-                rg = st.rng[pid];
+                rg = kNrc ? st.rng[pid] : st.q_rng[b & 1][R + q];
             }
             Payload Rp;
             Rp.hitValue = Rp.scatterDir = Rp.emittance = f3(0.0f);
@@ -420,14 +422,22 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 if (!Rp.needScatter || Rp.t < 0.0f) cont = false;
             }
             if (stop_after) cont = false;
-            st.tp[pid] = f4(tp, Rp.t);
+            // .w of the radiance: volume_dis while the path goes on, its last Ray.t once it has
+            // ended (wf_finish reads it); frames with a radiance cache keep Ray.t in tp
+            const float rad_w = (kNrc || cont) ? Rp.volume_dis : Rp.t;
             if (kNrc || !shadow) {
-                st.rad[pid] = f4(rad, Rp.volume_dis);
+                st.rad[pid] = f4(rad, rad_w);
             } else {  // the shadow kernel writes the radiance: E + C when the light is visible (rchit:338-350)
-                sh_blocked = f4(rad + tp_before * se, Rp.volume_dis);
-                sh_lit = f4(rad + tp_before * (se + sc), Rp.volume_dis);
+                sh_blocked = f4(rad + tp_before * se, rad_w);
+                sh_lit = f4(rad + tp_before * (se + sc), rad_w);
             }
-            if (cont) st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);  // read again only by a next bounce
+            if constexpr (kNrc) {
+                st.tp[pid] = f4(tp, Rp.t);
+                if (cont) st.rng[pid] = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);  // read again only by a next bounce
+            } else {  // written beside the next extension ray, in queue order
+                q_tp_next = f4(tp, Rp.t);
+                q_rng_next = make_uint4(rg.x, Rp.rngState.w, rg.z, 0u);
+            }
             nxt_o = Rp.hitPoint;
             nxt_d = Rp.scatterDir;
             nseed = Rp.RandomSeed;
@@ -444,6 +454,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         }
         if (cont) {
             no[slot] = f4(nxt_o, __uint_as_float(nseed));
+            if constexpr (!kNrc) {
+                st.q_tp[(b + 1) & 1][R + slot] = q_tp_next;
+                st.q_rng[(b + 1) & 1][R + slot] = q_rng_next;
+            }
             nd[slot] = f4(nxt_d, __uint_as_float(word));
         }
         if (shadow) {
@@ -520,7 +534,8 @@ GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave*
     float last_t = acc.w;
     for (uint32_t j = 0; j < sg.k; ++j) {
         const uint32_t pid = sg.path0 + li + j * sg.npw;
-        const float3 r = f3(st.rad[pid]);
+        const float4 r4 = st.rad[pid];
+        const float3 r = f3(r4);
         if (J.out.sample_radiance) {
             float* sr = J.out.sample_radiance + ((size_t)pix * J.ns + sg.si0 + j) * 3;
             sr[0] = r.x;
@@ -528,7 +543,7 @@ GB_D void finish_body(const Wv& w, const WfState& st, uint32_t i, const NrcWave*
             sr[2] = r.z;
         }
         sum += r;
-        last_t = st.tp[pid].w;
+        last_t = kNrc ? st.tp[pid].w : r4.w;
         if constexpr (kNrc) {  // training sample: suffix radiance / throughput at the vertex
             const float4 sp = nrc->snap_pos[pid];
             if (sp.w != 0.0f) {
