@@ -40,15 +40,18 @@ struct WfState {
     uint32_t* hit_prim;
     float4* q_tp[2];    // beside the extension queues: the path's throughput, Ray.t
     uint4* q_rng[2];    //   pixel-stream counter, ray-stream counter, ray-stream z
-    float4* rad;        // per path: radiance, volume_dis (Ray.t once the path has ended)
+    float4* q_rad[2];   //   radiance, volume_dis
+    float4* rad;        // per path, once it has ended: radiance, last Ray.t (the whole way in cache frames)
     float4* tp;         //   throughput, Ray.t, and
     uint4* rng;         //   RNG counters, in frames with a radiance cache (which reads them by path id)
     float4* sh_o;       // shadow queue: origin, tmax
     float4* sh_d;       //   direction, path id
     // the path's radiance (and volume_dis) after this vertex if the shadow ray
-    // is blocked / unblocked; in frames with a radiance cache (kShadowDelta)
-    // instead emission E + throughput.x / NEE term C + throughput.y, added to
-    // the radiance by the shadow kernel with throughput.z from sh_tp
+    // is blocked / unblocked, and in sh_tp the bits of where it goes (the
+    // path's next queue slot | kDstQueue, or its path id if it has ended); in
+    // frames with a radiance cache (kShadowDelta) instead emission E +
+    // throughput.x / NEE term C + throughput.y, added to the path's radiance by
+    // the shadow kernel with throughput.z from sh_tp
     float4* sh_e;
     float4* sh_c;
     float* sh_tp;
@@ -57,6 +60,8 @@ struct WfState {
 };
 // WaveJob::flags bit: the job's shadow records hold deltas (sh_e / sh_c).
 constexpr uint32_t kShadowDelta = 0x80000000u;
+// sh_tp destination bit: the radiance goes to q_rad at that queue slot.
+constexpr uint32_t kDstQueue = 0x80000000u;
 
 // One job of a wave: a scene, its UBO and its outputs.  The job's paths are
 // the contiguous range [path0, path0 + npaths) of the wave; its queues live

@@ -316,7 +316,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         float stmax = 0.0f;
         uint32_t word = 0, nseed = 0;
         float4 sh_blocked = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh_lit = sh_blocked;  // radiance after this vertex, shadow ray blocked / not
-        float4 q_tp_next = sh_blocked;  // throughput and Ray.t for the next bounce's queue
+        float4 q_tp_next = sh_blocked, q_rad_next = sh_blocked;  // throughput, radiance for the next bounce's queue
         uint4 q_rng_next = make_uint4(0u, 0u, 0u, 0u);
         if (active) {
             const float4 d4 = rd[q];
@@ -331,7 +331,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
                 initial_state(ubo, st.ray_o[0][R + q].w, P.sg->sample0 + P.j, tp4, rad4, hp4, rg);
             } else {  // the hit point is this ray's origin, which carries RandomSeed
                 tp4 = kNrc ? st.tp[pid] : st.q_tp[b & 1][R + q];
-                rad4 = st.rad[pid];
+                rad4 = kNrc ? st.rad[pid] : st.q_rad[b & 1][R + q];
                 hp4 = st.ray_o[b & 1][R + q];
                 rg = kNrc ? st.rng[pid] : st.q_rng[b & 1][R + q];
             }
@@ -425,8 +425,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             // .w of the radiance: volume_dis while the path goes on, its last Ray.t once it has
             // ended (wf_finish reads it); frames with a radiance cache keep Ray.t in tp
             const float rad_w = (kNrc || cont) ? Rp.volume_dis : Rp.t;
-            if (kNrc || !shadow) {
+            if (kNrc || (!shadow && !cont)) {
                 st.rad[pid] = f4(rad, rad_w);
+            } else if (!shadow) {
+                q_rad_next = f4(rad, rad_w);
             } else {  // the shadow kernel writes the radiance: E + C when the light is visible (rchit:338-350)
                 sh_blocked = f4(rad + tp_before * se, rad_w);
                 sh_lit = f4(rad + tp_before * (se + sc), rad_w);
@@ -457,6 +459,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             if constexpr (!kNrc) {
                 st.q_tp[(b + 1) & 1][R + slot] = q_tp_next;
                 st.q_rng[(b + 1) & 1][R + slot] = q_rng_next;
+                if (!shadow) st.q_rad[(b + 1) & 1][R + slot] = q_rad_next;
             }
             nd[slot] = f4(nxt_d, __uint_as_float(word));
         }
@@ -470,6 +473,7 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
             } else {
                 st.sh_e[R + sslot] = sh_blocked;
                 st.sh_c[R + sslot] = sh_lit;
+                st.sh_tp[R + sslot] = __uint_as_float(cont ? slot | kDstQueue : word & kPidMask);
             }
         }
     }
@@ -503,11 +507,14 @@ GB_D void shadow_body(const Wv& w, const WfState& st, uint32_t b, uint32_t jb) {
             }
         },
         [&](uint32_t q, bool occluded, const Hit&) {
-            const uint32_t pid = __float_as_uint(sd[q].w) & kPidMask;
-            if (!(J.flags & kShadowDelta)) {  // the record holds both outcomes
-                st.rad[pid] = occluded ? st.sh_e[R + q] : st.sh_c[R + q];
+            if (!(J.flags & kShadowDelta)) {  // the record holds both outcomes and where they go
+                const uint32_t dst = __float_as_uint(st.sh_tp[R + q]);
+                const float4 v = occluded ? st.sh_e[R + q] : st.sh_c[R + q];
+                if (dst & kDstQueue) st.q_rad[(b + 1) & 1][R + (dst & ~kDstQueue)] = v;
+                else st.rad[dst] = v;
                 return;
             }
+            const uint32_t pid = __float_as_uint(sd[q].w) & kPidMask;
             const float4 e4 = st.sh_e[R + q], c4 = st.sh_c[R + q];
             const float tpz = st.sh_tp[R + q];
             float3 e = f3(e4);
