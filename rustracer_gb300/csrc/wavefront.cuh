@@ -315,8 +315,10 @@ GB_D void shade_body(const Wv& w, const WfState& st, uint32_t b, const NrcWave* 
         float3 tp_before = f3(0.0f);
         float stmax = 0.0f;
         uint32_t word = 0, nseed = 0;
-        float4 sh_blocked = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh_lit = sh_blocked;  // radiance after this vertex, shadow ray blocked / not
-        float4 q_tp_next = sh_blocked, q_rad_next = sh_blocked;  // throughput, radiance for the next bounce's queue
+        // radiance after this vertex with the shadow ray blocked / not; throughput, radiance and RNG
+        // counters for the next bounce's queue
+        float4 sh_blocked = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh_lit = sh_blocked;
+        float4 q_tp_next = sh_blocked, q_rad_next = sh_blocked;
         uint4 q_rng_next = make_uint4(0u, 0u, 0u, 0u);
         if (active) {
             const float4 d4 = rd[q];
