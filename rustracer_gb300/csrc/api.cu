@@ -87,7 +87,7 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t f4 = al((size_t)cap * sizeof(float4)), u1 = al((size_t)cap * 4);
     const size_t counts = al((size_t)kMaxWaveJobs * kWfCounters * sizeof(uint32_t));
-    const size_t bytes = 18 * f4 + 2 * u1 + counts;
+    const size_t bytes = 16 * f4 + 2 * u1 + counts;
     if (c->wf.cap < cap || c->wf_mem.bytes < bytes) {
         cudaError_t e = c->wf_mem.alloc(bytes);
         if (e != cudaSuccess) {
@@ -108,9 +108,12 @@ cudaError_t wavefront_reserve(gbrt_ctx* c, uint32_t cap, size_t npix) {
         w.q_rng[1] = (uint4*)take(f4);
         w.q_rad[0] = (float4*)take(f4);
         w.q_rad[1] = (float4*)take(f4);
-        w.tp = (float4*)take(f4);
+        // frames with a radiance cache keep throughput and RNG counters by path id and never touch
+        // the queue-ordered copies; other frames never touch the by-path-id ones (a camera of a
+        // frame without bounces writes tp, which no shade reads): they share memory
+        w.tp = w.q_tp[0];
+        w.rng = w.q_rng[0];
         w.rad = (float4*)take(f4);
-        w.rng = (uint4*)take(f4);
         w.sh_o = (float4*)take(f4);
         w.sh_d = (float4*)take(f4);
         w.sh_e = (float4*)take(f4);
