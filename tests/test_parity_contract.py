@@ -70,3 +70,16 @@ def test_rows_band(ico):
     g = band["samples"].reshape(32, 48, 4, 3)[8:16]
     c = parity.classify(g, band, orc, ubo, 48, 32, rows=(8, 16))
     assert c["n"] == 8 * 48 * 4 and c["mismatched"] == 0
+
+
+def test_nudge_draws_differ(ico):
+    """Each draw index gives other nudge signs (the contract tries several
+    per size); the oracle rejects sizes and draws outside 16 bits."""
+    sd, ubo, orc, ref = ico
+    a = orc.render(ubo, 48, 32, want_samples=True, nudge_ulps=2, nudge_draw=0)["samples"]
+    b = orc.render(ubo, 48, 32, want_samples=True, nudge_ulps=2, nudge_draw=1)["samples"]
+    again = orc.render(ubo, 48, 32, want_samples=True, nudge_ulps=2, nudge_draw=1)["samples"]
+    assert np.array_equal(b.view(np.uint32), again.view(np.uint32))  # deterministic
+    assert not np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    with pytest.raises(AssertionError):
+        orc.render(ubo, 48, 32, want_samples=True, nudge_ulps=1, nudge_draw=1 << 16)
